@@ -1,0 +1,453 @@
+"""Python host mirror of 3photons-rust over the GB300 event kernel.
+
+The reference program (src/main.rs:75-145) reads `valeurs` with
+``Configuration::load`` (src/config.rs:57-128), hands the event loop to
+``scheduling::run_simulation`` (src/scheduling/mod.rs:31-59), and prints /
+writes the results with ``FinalResults::eric``/``fawzi`` and
+``output::dump_results`` (src/resfin.rs:66-194, src/output.rs:30-177). This
+module offers the same steps under the same names; the event loop runs in
+``libtp_gb300.so`` (CUDA kernels for sm_103a behind the C ABI of
+include/tp_gpu.h), and everything else calls the library's host functions.
+
+There is no CPU fallback: if the library or a CUDA device is missing, the
+GPU entry points raise.
+"""
+import ctypes
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtp_gb300.so")
+
+# ---- constants of include/tp_gpu.h -------------------------------------
+TP_OK = 0
+TP_ERR_INVALID = -1
+TP_ERR_UNSUPPORTED = -2
+TP_ERR_CUDA = -3
+TP_ERR_DEVICE = -4
+TP_ERR_TIMEOUT = -5
+TP_ERR_NO_DEVICE = -6
+TP_ERR_IO = -7
+TP_BATCH_SIZE = 10000
+TP_RNG_RANF = 0
+TP_RNG_XOSHIRO256P = 1
+TP_MODE_JUMP_PER_BATCH = 0x100
+TP_MODE_NO_PHOTON_SORTING = 0x200
+TP_PREC_FP64 = 0
+TP_PREC_FP32_MIXED = 1
+RANF_DEFAULT_SEED = 234612947
+XOSHIRO_DEFAULT_SEED = 12345
+
+ERROR_NAMES = {
+    TP_ERR_INVALID: "invalid argument",
+    TP_ERR_UNSUPPORTED: "unsupported",
+    TP_ERR_CUDA: "CUDA error",
+    TP_ERR_DEVICE: "device error flag",
+    TP_ERR_TIMEOUT: "device wait timed out",
+    TP_ERR_NO_DEVICE: "no CUDA device",
+    TP_ERR_IO: "I/O error",
+}
+
+
+class TPError(RuntimeError):
+    """A negative status returned by the library."""
+
+    def __init__(self, code, message=""):
+        self.code = code
+        super().__init__("%s (%d)%s" % (ERROR_NAMES.get(code, "error"), code, (": " + message) if message else ""))
+
+
+# ---- ctypes mirrors of the ABI structs -----------------------------------
+class CConfig(ctypes.Structure):
+    _fields_ = [
+        ("num_events", ctypes.c_uint64),
+        ("e_total", ctypes.c_double),
+        ("beam_photons_cut", ctypes.c_double),
+        ("photon_photon_cut", ctypes.c_double),
+        ("e_min", ctypes.c_double),
+        ("beam_photon_plane_cut", ctypes.c_double),
+        ("alpha", ctypes.c_double),
+        ("alpha_z", ctypes.c_double),
+        ("gev2_to_picobarn", ctypes.c_double),
+        ("m_z0", ctypes.c_double),
+        ("g_z0", ctypes.c_double),
+        ("sin2_weinberg", ctypes.c_double),
+        ("branching_ep_em", ctypes.c_double),
+        ("beta_plus", ctypes.c_double),
+        ("beta_minus", ctypes.c_double),
+        ("num_bins", ctypes.c_int32),
+        ("impr", ctypes.c_int32),
+        ("plot", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class CBatchSoa(ctypes.Structure):
+    _fields_ = [
+        ("selected", ctypes.c_void_p),
+        ("spm2", ctypes.c_void_p),
+        ("vars", ctypes.c_void_p),
+        ("sigma", ctypes.c_void_p),
+        ("variance", ctypes.c_void_p),
+    ]
+
+
+class CEventDump(ctypes.Structure):
+    _fields_ = [
+        ("uniforms", ctypes.c_double * 12),
+        ("p_out", (ctypes.c_double * 4) * 3),
+        ("cut", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("m2_sums", ctypes.c_double * 5),
+    ]
+
+
+class CFinalResults(ctypes.Structure):
+    _fields_ = [
+        ("selected_events", ctypes.c_uint64),
+        ("spm2", (ctypes.c_double * 5) * 2),
+        ("vars", (ctypes.c_double * 5) * 2),
+        ("sigma", ctypes.c_double),
+        ("prec", ctypes.c_double),
+        ("variance", ctypes.c_double),
+        ("beta_min", ctypes.c_double),
+        ("ss_p", ctypes.c_double),
+        ("inc_ss_p", ctypes.c_double),
+        ("ss_m", ctypes.c_double),
+        ("inc_ss_m", ctypes.c_double),
+    ]
+
+
+DUMP_DTYPE = np.dtype(
+    [("uniforms", "<f8", (12,)), ("p_out", "<f8", (3, 4)), ("cut", "<i4"), ("reserved", "<i4"), ("m2_sums", "<f8", (5,))]
+)
+assert DUMP_DTYPE.itemsize == ctypes.sizeof(CEventDump)
+
+_lib = None
+
+
+def library():
+    """Loads libtp_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libtp_gb300.so is missing: run __graft_entry__.build() first")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    vp, u64, i32, dbl = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_double
+    sig = {
+        "tp_create": (vp, [i32, P(ctypes.c_int)]),
+        "tp_destroy": (None, [vp]),
+        "tp_last_error": (ctypes.c_char_p, [vp]),
+        "tp_run_batches": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa)]),
+        "tp_run_batches_async": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
+        "tp_dump_events": (i32, [vp, P(CConfig), i32, u64, u64, u64, vp]),
+        "tp_set_events_per_thread": (i32, [vp, i32]),
+        "tp_profile": (i32, [vp, i32]),
+        "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
+        "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
+        "tp_xoshiro_state_at": (i32, [u64, u64, u64, P(ctypes.c_uint64)]),
+        "tp_ranf_state_at": (i32, [ctypes.c_int32, u64, P(ctypes.c_int32), P(ctypes.c_int32)]),
+        "tp_config_load": (i32, [ctypes.c_char_p, P(CConfig), ctypes.c_char_p, ctypes.c_size_t]),
+        "tp_event_weight": (i32, [dbl, P(ctypes.c_double)]),
+        "tp_merge_finalize": (i32, [P(CConfig), P(CBatchSoa), u64, P(CFinalResults)]),
+        "tp_format_res_data": (i32, [P(CConfig), P(CFinalResults), ctypes.c_char_p, ctypes.c_size_t]),
+        "tp_write_res_data": (i32, [P(CConfig), P(CFinalResults), ctypes.c_char_p]),
+        "tp_write_res_times": (i32, [P(CConfig), dbl, ctypes.c_char_p, ctypes.c_char_p]),
+        "tp_append_pil_mc": (i32, [P(CConfig), P(CFinalResults), ctypes.c_char_p, ctypes.c_char_p]),
+        "tp_format_report": (i32, [P(CConfig), P(CFinalResults), ctypes.c_char_p, ctypes.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(lib, name):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(code, ctx=None):
+    if code != TP_OK:
+        msg = library().tp_last_error(ctx).decode() if code != TP_OK else ""
+        raise TPError(code, msg)
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+# ---- Configuration (src/config.rs) ----------------------------------------
+class Configuration:
+    """The 18 items of `valeurs` (src/config.rs:152-198)."""
+
+    FIELDS = [f for f, _ in CConfig._fields_ if f != "reserved"]
+
+    def __init__(self, c=None, **kw):
+        self.c = c if c is not None else CConfig()
+        for k, v in kw.items():
+            setattr(self.c, k, v)
+
+    def __getattr__(self, name):
+        if name != "c" and name in Configuration.FIELDS:
+            return getattr(self.c, name)
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in Configuration.FIELDS:
+            setattr(self.c, name, value)
+        else:
+            object.__setattr__(self, name, value)
+
+    @classmethod
+    def load(cls, path="valeurs", echo=True):
+        """Configuration::load: parse, echo (like the reference), check."""
+        c = CConfig()
+        buf = ctypes.create_string_buffer(4096)
+        st = library().tp_config_load(path.encode(), ctypes.byref(c), buf, len(buf))
+        if echo:
+            print(buf.value.decode(), end="")
+        _check(st)
+        return cls(c)
+
+    @property
+    def num_batches(self):
+        return (self.c.num_events + TP_BATCH_SIZE - 1) // TP_BATCH_SIZE
+
+    def replace(self, **kw):
+        c = CConfig()
+        ctypes.pointer(c)[0] = self.c
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return Configuration(c)
+
+    def as_dict(self):
+        return {f: getattr(self.c, f) for f in Configuration.FIELDS}
+
+
+def rng_flags(rng="ranf", jump_per_batch=False, sorting=True):
+    kind = {"ranf": TP_RNG_RANF, "xoshiro": TP_RNG_XOSHIRO256P, "standard-random": TP_RNG_XOSHIRO256P}[rng]
+    if jump_per_batch:
+        kind |= TP_MODE_JUMP_PER_BATCH
+    if not sorting:
+        kind |= TP_MODE_NO_PHOTON_SORTING
+    return kind
+
+
+def default_seed(rng):
+    return RANF_DEFAULT_SEED if rng == "ranf" else XOSHIRO_DEFAULT_SEED
+
+
+# ---- per-batch accumulators ------------------------------------------------
+class BatchAccumulators:
+    """ResultsAccumulator sums of consecutive batches, structure of arrays
+    (src/resacc.rs:18-34): selected[n], spm2[5, n], vars[5, n], sigma[n],
+    variance[n]."""
+
+    def __init__(self, n):
+        self.n = n
+        self.selected = np.zeros(n, np.uint64)
+        self.spm2 = np.zeros((5, n), np.float64)
+        self.vars = np.zeros((5, n), np.float64)
+        self.sigma = np.zeros(n, np.float64)
+        self.variance = np.zeros(n, np.float64)
+
+    def soa(self):
+        return CBatchSoa(_ptr(self.selected), _ptr(self.spm2), _ptr(self.vars), _ptr(self.sigma), _ptr(self.variance))
+
+    @classmethod
+    def concatenate(cls, parts):
+        out = cls(sum(p.n for p in parts))
+        i = 0
+        for p in parts:
+            out.selected[i:i + p.n] = p.selected
+            out.spm2[:, i:i + p.n] = p.spm2
+            out.vars[:, i:i + p.n] = p.vars
+            out.sigma[i:i + p.n] = p.sigma
+            out.variance[i:i + p.n] = p.variance
+            i += p.n
+        return out
+
+    def as_array(self):
+        """(n, 13) float64 view: selected, spm2[5], vars[5], sigma, variance."""
+        return np.concatenate([self.selected[None].astype(np.float64), self.spm2, self.vars,
+                               self.sigma[None], self.variance[None]]).T.copy()
+
+    @classmethod
+    def from_array(cls, a):
+        a = np.asarray(a, np.float64)
+        out = cls(a.shape[0])
+        out.selected[:] = a[:, 0].astype(np.uint64)
+        out.spm2[:] = a[:, 1:6].T
+        out.vars[:] = a[:, 6:11].T
+        out.sigma[:] = a[:, 11]
+        out.variance[:] = a[:, 12]
+        return out
+
+
+# ---- FinalResults (src/resfin.rs) -------------------------------------------
+class FinalResults:
+    def __init__(self, cfg, c):
+        self.cfg = cfg
+        self.c = c
+        self.selected_events = c.selected_events
+        self.spm2 = np.array([[c.spm2[s][k] for k in range(5)] for s in range(2)])
+        self.vars = np.array([[c.vars[s][k] for k in range(5)] for s in range(2)])
+        for f in ("sigma", "prec", "variance", "beta_min", "ss_p", "inc_ss_p", "ss_m", "inc_ss_m"):
+            setattr(self, f, getattr(c, f))
+
+    def report(self):
+        """"IBegin" + eric() + fawzi() text (src/resfin.rs:66-194)."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = library().tp_format_report(ctypes.byref(self.cfg.c), ctypes.byref(self.c), buf, len(buf))
+        if n < 0:
+            _check(n)
+        return buf.value.decode()
+
+    def res_data(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = library().tp_format_res_data(ctypes.byref(self.cfg.c), ctypes.byref(self.c), buf, len(buf))
+        if n < 0:
+            _check(n)
+        return buf.value.decode()
+
+
+def merge_finalize(cfg, acc):
+    """ResultsAccumulator::merge in batch order, then ::finalize."""
+    res = CFinalResults()
+    soa = acc.soa()
+    _check(library().tp_merge_finalize(ctypes.byref(cfg.c), ctypes.byref(soa), acc.n, ctypes.byref(res)))
+    return FinalResults(cfg, res)
+
+
+# ---- the GPU event loop ------------------------------------------------------
+class Context:
+    """One CUDA device context (tp_create / tp_destroy)."""
+
+    def __init__(self, device=0):
+        lib = library()
+        st = ctypes.c_int(0)
+        self.h = lib.tp_create(device, ctypes.byref(st))
+        if not self.h:
+            raise TPError(st.value, lib.tp_last_error(None).decode())
+        self.device = device
+
+    def close(self):
+        if self.h:
+            library().tp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, code):
+        if code != TP_OK:
+            raise TPError(code, library().tp_last_error(self.h).decode())
+
+    def set_events_per_thread(self, ept):
+        self.check(library().tp_set_events_per_thread(self.h, ept))
+
+    def profile(self, enable=True):
+        self.check(library().tp_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        """(event-kernel ms, launches, seed-kernel ms, launches) since profile(True)."""
+        em, el, sm, sl = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_double(), ctypes.c_uint64()
+        self.check(library().tp_profile_read(self.h, ctypes.byref(em), ctypes.byref(el), ctypes.byref(sm),
+                                             ctypes.byref(sl)))
+        return em.value, el.value, sm.value, sl.value
+
+    def probe_fp64(self):
+        """{'dfma_flops': flop/s, 'log'|'sincos'|'sqrt'|'div': DFMA-equivalents}."""
+        out = (ctypes.c_double * 5)()
+        self.check(library().tp_probe_fp64(self.h, out))
+        return {"dfma_flops": out[0], "log": out[1], "sincos": out[2], "sqrt": out[3], "div": out[4]}
+
+    def run_batches(self, cfg, first_batch, n_batches, rng="ranf", seed=None, jump_per_batch=False, sorting=True,
+                    precision=TP_PREC_FP64, out=None):
+        """Per-batch accumulators of batches [first_batch, first_batch + n)."""
+        seed = default_seed(rng) if seed is None else seed
+        acc = out if out is not None else BatchAccumulators(n_batches)
+        soa = acc.soa()
+        self.check(library().tp_run_batches(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+                                            seed, first_batch, n_batches, precision, ctypes.byref(soa)))
+        return acc
+
+    def run_batches_device(self, cfg, first_batch, n_batches, out_ptrs, stream=0, rng="ranf", seed=None,
+                           jump_per_batch=False, sorting=True, precision=TP_PREC_FP64):
+        """Queues the batches on `stream` writing DEVICE arrays given as five
+        raw pointers (selected, spm2, vars, sigma, variance)."""
+        seed = default_seed(rng) if seed is None else seed
+        soa = CBatchSoa(*[ctypes.c_void_p(p) for p in out_ptrs])
+        self.check(library().tp_run_batches_async(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+                                                  seed, first_batch, n_batches, precision, ctypes.byref(soa),
+                                                  ctypes.c_void_p(stream)))
+
+    def dump_events(self, cfg, first_event, n, rng="ranf", seed=None, jump_per_batch=False, sorting=True):
+        seed = default_seed(rng) if seed is None else seed
+        out = np.zeros(n, DUMP_DTYPE)
+        self.check(library().tp_dump_events(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+                                            seed, first_event, n, ctypes.c_void_p(out.ctypes.data)))
+        return out
+
+
+def run_simulation(cfg, rng="ranf", seed=None, jump_per_batch=False, sorting=True, precision=TP_PREC_FP64,
+                   device=0, ctx=None):
+    """scheduling::run_simulation (src/scheduling/mod.rs:31-59): every batch
+    on the GPU, merged in batch order on the host, finalised."""
+    own = ctx is None
+    ctx = ctx or Context(device)
+    try:
+        acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng, seed, jump_per_batch, sorting, precision)
+    finally:
+        if own:
+            ctx.close()
+    return merge_finalize(cfg, acc)
+
+
+def run_simulation_sharded(cfg, rank, world_size, run_batches, all_gather, **kw):
+    """Batch-range sharding over `world_size` processes with no data-path
+    collective: rank r integrates batches [lo_r, hi_r); the per-batch
+    accumulators (13 numbers per batch) are gathered once and merged in batch
+    order, so the result equals the single-process run bit for bit.
+
+    run_batches(first_batch, n) -> BatchAccumulators; all_gather(ndarray) ->
+    list of ndarrays, one per rank (e.g. torch.distributed.all_gather_object).
+    """
+    nb = cfg.num_batches
+    lo = nb * rank // world_size
+    hi = nb * (rank + 1) // world_size
+    part = run_batches(lo, hi - lo) if hi > lo else BatchAccumulators(0)
+    parts = [BatchAccumulators.from_array(a) for a in all_gather(part.as_array())]
+    return merge_finalize(cfg, BatchAccumulators.concatenate(parts))
+
+
+def dump_results(cfg, res, elapsed_seconds, directory=".", timestamp=None):
+    """output::dump_results (src/output.rs:30-177): prints the report and
+    writes res.times, res.data and appends pil.mc."""
+    print(res.report(), end="")
+    lib = library()
+    ts = timestamp.encode() if timestamp else None
+    _check(lib.tp_write_res_times(ctypes.byref(cfg.c), elapsed_seconds, ts, os.path.join(directory, "res.times").encode()))
+    _check(lib.tp_write_res_data(ctypes.byref(cfg.c), ctypes.byref(res.c), os.path.join(directory, "res.data").encode()))
+    _check(lib.tp_append_pil_mc(ctypes.byref(cfg.c), ctypes.byref(res.c), ts, os.path.join(directory, "pil.mc").encode()))
+
+
+def main(valeurs="valeurs", directory=".", **kw):
+    """main() (src/main.rs:75-145)."""
+    cfg = Configuration.load(valeurs)
+    t0 = time.perf_counter()
+    res = run_simulation(cfg, **kw)
+    dump_results(cfg, res, time.perf_counter() - t0, directory)
+    return res

@@ -1,0 +1,476 @@
+// tp_capi.cpp — the C ABI of include/tp_gpu.h around the kernels: context,
+// device buffers, jump-ahead tables, batching of launches, error reporting.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tp_internal.h"
+#include "tp_rng.h"
+
+namespace {
+
+using namespace tp;
+
+thread_local std::string g_create_error;
+
+// Batches per launch: bounds the device scratch (batch start states) to
+// 64 Ki batches = 14.7 MB (ranf) or 2 MB (xoshiro).
+constexpr uint64_t kChunk = 1ull << 16;
+constexpr int kTpb = 256;      // threads per CTA (one batch per CTA)
+constexpr int kDefaultEpt = 40;  // xoshiro: events per thread (250 x 40)
+
+struct Tables {
+  std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
+  std::vector<uint32_t> ranf;                         // 64 x 55
+};
+
+const Tables& host_tables() {
+  static Tables t;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    t.xo_batch.resize(256);
+    t.xo_jump.resize(256);
+    t.xo_draw.resize(256);
+    Gf2Poly pb = gf2_xpow(kDrawsPerBatch), pj = gf2_xpow2k(128), pd = gf2_xpow(kDrawsPerEvent);
+    for (int k = 0; k < 64; ++k) {
+      for (int w = 0; w < 4; ++w) {
+        t.xo_batch[4 * k + w] = pb.w[w];
+        t.xo_jump[4 * k + w] = pj.w[w];
+        t.xo_draw[4 * k + w] = pd.w[w];
+      }
+      pb = gf2_mulmod(pb, pb);
+      pj = gf2_mulmod(pj, pj);
+      pd = gf2_mulmod(pd, pd);
+    }
+    t.ranf.resize(64 * 55);
+    RanfPoly r = ranf_xpow(55);
+    for (int k = 0; k < 64; ++k) {
+      for (int i = 0; i < 55; ++i) t.ranf[55 * k + i] = r.c[i];
+      r = ranf_mulmod(r, r);
+    }
+  });
+  return t;
+}
+
+}  // namespace
+
+struct tp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int ept = kDefaultEpt;
+  uint64_t* d_xo_batch = nullptr;
+  uint64_t* d_xo_jump = nullptr;
+  uint64_t* d_xo_draw = nullptr;
+  uint32_t* d_ranf_tab = nullptr;
+  uint64_t* d_thread_poly = nullptr;
+  int thread_poly_ept = 0;
+  int32_t* d_ranf_window = nullptr;
+  int64_t ranf_window_seed = -1;
+  void* d_state = nullptr;
+  void* d_out = nullptr;
+  size_t out_bytes = 0;
+  void* d_dump = nullptr;
+  size_t dump_bytes = 0;
+  unsigned int* d_err = nullptr;
+  // optional CUDA-event timing of every kernel launch (tp_profile)
+  int prof = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_marks;  // (kind, start/end)
+  size_t ev_used = 0;
+
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return TP_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return TP_ERR_CUDA;
+  }
+};
+
+namespace {
+
+int ensure(tp_ctx* c, void** p, size_t* have, size_t need, const char* what) {
+  if (*have >= need) return TP_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  int st = c->cuda(cudaMalloc(p, need), what);
+  if (st == TP_OK) *have = need;
+  return st;
+}
+
+int ensure_thread_poly(tp_ctx* c, int ept) {
+  if (c->thread_poly_ept == ept) return TP_OK;
+  std::vector<uint64_t> h(4 * kTpb);
+  const Gf2Poly step = gf2_xpow((uint64_t)kDrawsPerEvent * ept);
+  Gf2Poly cur{{1, 0, 0, 0}};
+  for (int j = 0; j < kTpb; ++j) {
+    for (int w = 0; w < 4; ++w) h[4 * j + w] = cur.w[w];
+    cur = gf2_mulmod(cur, step);
+  }
+  int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
+                   "upload thread polynomials");
+  if (st) return st;
+  st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
+  if (st == TP_OK) c->thread_poly_ept = ept;
+  return st;
+}
+
+// blocks 0 and 1 of a ranf stream (110 values) for the one-stream mode
+int ensure_ranf_window(tp_ctx* c, int32_t seed) {
+  if (c->ranf_window_seed == (int64_t)seed) return TP_OK;
+  int32_t w[110];
+  ranf_seeded(seed, w);
+  if (!ranf_canonical(w))
+    return c->fail(TP_ERR_UNSUPPORTED, "ranf seed gives a state outside [0, 1e9): no jump-ahead");
+  for (int i = 0; i < 55; ++i) w[55 + i] = w[i];
+  ranf_reset(w + 55);
+  int st = c->cuda(cudaMemcpyAsync(c->d_ranf_window, w, sizeof w, cudaMemcpyHostToDevice, c->stream),
+                   "upload ranf window");
+  if (st) return st;
+  st = c->cuda(cudaStreamSynchronize(c->stream), "upload ranf window");
+  if (st == TP_OK) c->ranf_window_seed = seed;
+  return st;
+}
+
+int check_kind(tp_ctx* c, int rng_kind) {
+  const int kind = rng_kind & TP_RNG_KIND_MASK;
+  if (kind != TP_RNG_RANF && kind != TP_RNG_XOSHIRO256P) return c->fail(TP_ERR_INVALID, "unknown rng kind");
+  if (rng_kind & ~(TP_RNG_KIND_MASK | TP_MODE_JUMP_PER_BATCH | TP_MODE_NO_PHOTON_SORTING))
+    return c->fail(TP_ERR_INVALID, "unknown mode flag");
+  return TP_OK;
+}
+
+int check_seed(tp_ctx* c, int rng_kind, uint64_t seed) {
+  if ((rng_kind & TP_RNG_KIND_MASK) == TP_RNG_RANF && seed > 0x7fffffffull)
+    return c->fail(TP_ERR_INVALID, "ranf seed must fit in i32");
+  return TP_OK;
+}
+
+// Queues the batches on `stream`; `out` holds device pointers (stride n).
+int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+              uint64_t n_batches, int precision, const BatchOut& out, cudaStream_t stream) {
+  if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
+  if (int st = check_kind(c, rng_kind)) return st;
+  if (int st = check_seed(c, rng_kind, seed)) return st;
+  if (n_batches == 0) return TP_OK;
+  if (first_batch > (1ull << 46) || n_batches > (1ull << 46))
+    return c->fail(TP_ERR_INVALID, "batch range too large");
+  if (precision != TP_PREC_FP64)
+    return c->fail(TP_ERR_UNSUPPORTED, "precision not available in this build");
+  const int kind = rng_kind & TP_RNG_KIND_MASK;
+  const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
+  KParams kp{};
+  make_ev_const(*cfg, rng_kind & ~TP_RNG_KIND_MASK, &kp.k);
+  kp.num_events = cfg->num_events;
+  kp.precision = precision;
+  kp.err = c->d_err;
+  kp.ept = c->ept;
+  if (kind == TP_RNG_XOSHIRO256P) {
+    if (int st = ensure_thread_poly(c, c->ept)) return st;
+  } else if (!jpb) {
+    if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
+  }
+  kp.thread_poly = c->d_thread_poly;
+  uint64_t start[4];
+  xoshiro_seed(seed, start);
+  for (uint64_t c0 = 0; c0 < n_batches; c0 += kChunk) {
+    const uint64_t cn = n_batches - c0 < kChunk ? n_batches - c0 : kChunk;
+    const uint64_t fb = first_batch + c0;
+    int st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
+    if (kind == TP_RNG_XOSHIRO256P)
+      st = launch_seed_xoshiro(start, jpb ? c->d_xo_jump : c->d_xo_batch, fb, cn,
+                               static_cast<uint64_t*>(c->d_state), stream);
+    else
+      st = launch_seed_ranf(jpb, (int32_t)seed, c->d_ranf_window, c->d_ranf_tab, fb, cn,
+                            static_cast<int32_t*>(c->d_state), stream);
+    if (e1) {
+      cudaEventRecord(e1, stream);
+      c->prof_marks.push_back({0, {e0, e1}});
+      e0 = e1 = nullptr;
+    }
+    if (st) return c->fail(st, std::string("seed launch: ") + cudaGetErrorString(cudaGetLastError()));
+    kp.first_batch = fb;
+    kp.n_batches = cn;
+    kp.batch_state = c->d_state;
+    kp.out = out;
+    kp.out.selected = out.selected + c0;
+    kp.out.spm2 = out.spm2 + c0;
+    kp.out.vars = out.vars + c0;
+    kp.out.sigma = out.sigma + c0;
+    kp.out.variance = out.variance + c0;
+    // xoshiro: enough warps for ceil(10000 / ept) threads; ranf: rounds of 256
+    const int need = (kBatch + c->ept - 1) / c->ept;
+    const int tpb = kind == TP_RNG_XOSHIRO256P ? ((need + 31) / 32) * 32 : kTpb;
+    if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
+    st = launch_events(rng_kind, kp, tpb, stream);
+    if (e1) {
+      cudaEventRecord(e1, stream);
+      c->prof_marks.push_back({1, {e0, e1}});
+    }
+    if (st) return c->fail(st, std::string("event launch: ") + cudaGetErrorString(cudaGetLastError()));
+  }
+  return TP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tp_ctx* tp_create(int device, int* status) {
+  auto failc = [&](int code, const std::string& msg) -> tp_ctx* {
+    g_create_error = msg;
+    if (status) *status = code;
+    return nullptr;
+  };
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return failc(TP_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= n) return failc(TP_ERR_NO_DEVICE, "device index out of range");
+  if (cudaSetDevice(device) != cudaSuccess) return failc(TP_ERR_NO_DEVICE, "cudaSetDevice failed");
+  tp_ctx* c = new tp_ctx;
+  c->device = device;
+  const Tables& t = host_tables();
+  int st = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+  size_t dummy = 0;
+  void* p;
+  auto alloc = [&](void** dst, size_t bytes, const char* what) {
+    if (st) return;
+    st = c->cuda(cudaMalloc(dst, bytes), what);
+  };
+  alloc((void**)&c->d_xo_batch, 256 * 8, "tables");
+  alloc((void**)&c->d_xo_jump, 256 * 8, "tables");
+  alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
+  alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
+  alloc((void**)&c->d_thread_poly, kTpb * 32, "tables");
+  alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
+  alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
+  alloc(&c->d_state, kChunk * 56 * 4, "batch states");
+  (void)dummy;
+  (void)p;
+  if (!st) st = c->cuda(cudaMemcpy(c->d_xo_batch, t.xo_batch.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st) st = c->cuda(cudaMemcpy(c->d_xo_jump, t.xo_jump.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st) st = c->cuda(cudaMemcpy(c->d_xo_draw, t.xo_draw.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st) st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), 64 * 55 * 4, cudaMemcpyHostToDevice), "tables");
+  if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
+  if (st) {
+    g_create_error = c->err;
+    if (status) *status = st;
+    tp_destroy(c);
+    return nullptr;
+  }
+  if (status) *status = TP_OK;
+  return c;
+}
+
+void tp_destroy(tp_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly,
+                  c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* tp_last_error(const tp_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int tp_run_batches_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+                         uint64_t n_batches, int precision, tp_batch_soa* out, void* stream) {
+  if (!c) return TP_ERR_INVALID;
+  if (!out || !out->selected || !out->spm2 || !out->vars || !out->sigma || !out->variance)
+    return c->fail(TP_ERR_INVALID, "null output array");
+  cudaSetDevice(c->device);
+  BatchOut o{out->selected, out->spm2, out->vars, out->sigma, out->variance, n_batches};
+  return run_async(c, cfg, rng_kind, seed, first_batch, n_batches, precision, o,
+                   stream ? (cudaStream_t)stream : c->stream);
+}
+
+int tp_run_batches(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+                   uint64_t n_batches, int precision, tp_batch_soa* out) {
+  if (!c) return TP_ERR_INVALID;
+  if (!out || !out->selected || !out->spm2 || !out->vars || !out->sigma || !out->variance)
+    return c->fail(TP_ERR_INVALID, "null output array");
+  if (n_batches == 0) return TP_OK;
+  if (n_batches > (1ull << 40)) return c->fail(TP_ERR_INVALID, "batch range too large");
+  cudaSetDevice(c->device);
+  const size_t n = n_batches;
+  if (int st = ensure(c, &c->d_out, &c->out_bytes, n * 13 * 8, "output buffers")) return st;
+  auto* sel = static_cast<uint64_t*>(c->d_out);
+  auto* f = reinterpret_cast<double*>(sel + n);
+  BatchOut o{sel, f, f + 5 * n, f + 10 * n, f + 11 * n, n};
+  int st = c->cuda(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "clear error word");
+  if (st) return st;
+  st = run_async(c, cfg, rng_kind, seed, first_batch, n_batches, precision, o, c->stream);
+  if (st) return st;
+  st = c->cuda(cudaMemcpyAsync(out->selected, sel, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->spm2, o.spm2, 5 * n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->vars, o.vars, 5 * n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->sigma, o.sigma, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->variance, o.variance, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  unsigned int herr = 0;
+  if (!st) st = c->cuda(cudaMemcpyAsync(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost, c->stream), "copy error word");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "run batches");
+  if (!st && herr) return c->fail(TP_ERR_DEVICE, "device error flag " + std::to_string(herr));
+  return st;
+}
+
+int tp_dump_events(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_event, uint64_t n,
+                   tp_event_dump* out) {
+  if (!c) return TP_ERR_INVALID;
+  if (!out) return c->fail(TP_ERR_INVALID, "null output array");
+  if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
+  if (int st = check_kind(c, rng_kind)) return st;
+  if (int st = check_seed(c, rng_kind, seed)) return st;
+  if (n == 0) return TP_OK;
+  if (n > (1ull << 26) || first_event > (1ull << 50)) return c->fail(TP_ERR_INVALID, "dump range too large");
+  cudaSetDevice(c->device);
+  const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
+  if ((rng_kind & TP_RNG_KIND_MASK) == TP_RNG_RANF && !jpb)
+    if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
+  if (int st = ensure(c, &c->d_dump, &c->dump_bytes, n * sizeof(tp_event_dump), "dump buffer")) return st;
+  EvConst k;
+  make_ev_const(*cfg, rng_kind & ~TP_RNG_KIND_MASK, &k);
+  uint64_t start[4];
+  xoshiro_seed(seed, start);
+  int st = c->cuda(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "clear error word");
+  if (st) return st;
+  st = launch_dump(rng_kind, k, start, c->d_ranf_window, (int32_t)seed, c->d_xo_draw, c->d_xo_jump, c->d_ranf_tab,
+                   first_event, n, static_cast<tp_event_dump*>(c->d_dump), c->d_err, c->stream);
+  if (st) return c->fail(st, std::string("dump launch: ") + cudaGetErrorString(cudaGetLastError()));
+  unsigned int herr = 0;
+  st = c->cuda(cudaMemcpyAsync(out, c->d_dump, n * sizeof(tp_event_dump), cudaMemcpyDeviceToHost, c->stream), "copy dump");
+  if (!st) st = c->cuda(cudaMemcpyAsync(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost, c->stream), "copy error word");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "dump events");
+  if (!st && herr) return c->fail(TP_ERR_UNSUPPORTED, "ranf batch seed outside [0, 1e9): no jump-ahead");
+  return st;
+}
+
+int tp_set_events_per_thread(tp_ctx* c, int ept) {
+  if (!c) return TP_ERR_INVALID;
+  if (ept <= 0 || (TP_BATCH_SIZE + ept - 1) / ept > kTpb) return c->fail(TP_ERR_INVALID, "events per thread out of range");
+  c->ept = ept;
+  return TP_OK;
+}
+
+int tp_profile(tp_ctx* c, int enable) {
+  if (!c) return TP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (enable) {
+    c->prof_marks.clear();
+    c->ev_used = 0;
+  }
+  c->prof = enable ? 1 : 0;
+  return TP_OK;
+}
+
+int tp_profile_read(tp_ctx* c, double* event_ms, uint64_t* event_launches, double* seed_ms, uint64_t* seed_launches) {
+  if (!c) return TP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  double ms[2] = {0.0, 0.0};
+  uint64_t cnt[2] = {0, 0};
+  for (auto& m : c->prof_marks) {
+    if (int st = c->cuda(cudaEventSynchronize(m.second.second), "profile")) return st;
+    float t = 0.f;
+    if (int st = c->cuda(cudaEventElapsedTime(&t, m.second.first, m.second.second), "profile")) return st;
+    ms[m.first] += t;
+    cnt[m.first] += 1;
+  }
+  if (event_ms) *event_ms = ms[1];
+  if (event_launches) *event_launches = cnt[1];
+  if (seed_ms) *seed_ms = ms[0];
+  if (seed_launches) *seed_launches = cnt[0];
+  c->prof_marks.clear();
+  c->ev_used = 0;
+  return TP_OK;
+}
+
+int tp_probe_fp64(tp_ctx* c, double out[5]) {
+  if (!c || !out) return TP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int sms = 0;
+  if (int st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "probe")) return st;
+  double* sink = nullptr;
+  if (int st = c->cuda(cudaMalloc(&sink, sizeof(double)), "probe")) return st;
+  cudaEvent_t a = c->next_event(), b = c->next_event();
+  const int blocks = sms * 8, tpb = 256;
+  const double threads = (double)blocks * tpb;
+  double per_op_s[5];
+  int st = TP_OK;
+  for (int op = 0; op < 5 && st == TP_OK; ++op) {
+    int iters = 16;
+    for (int rep = 0; rep < 8; ++rep) {
+      cudaEventRecord(a, c->stream);
+      st = launch_probe(op, iters, blocks, tpb, sink, c->stream);
+      cudaEventRecord(b, c->stream);
+      if (!st) st = c->cuda(cudaEventSynchronize(b), "probe");
+      if (st) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms > 20.f || rep == 7) {
+        per_op_s[op] = (ms * 1e-3) / (threads * 8.0 * iters);  // seconds per operation
+        break;
+      }
+      const double grow = ms > 0.01f ? 25.0 / ms : 64.0;
+      iters = (int)(iters * (grow > 64.0 ? 64.0 : grow)) + 1;
+    }
+  }
+  cudaFree(sink);
+  c->ev_used = 0;
+  if (st) return st;
+  out[0] = 2.0 / per_op_s[0];  // DFMA flop/s
+  for (int op = 1; op < 5; ++op) out[op] = per_op_s[op] / per_op_s[0];  // DFMA equivalents
+  return TP_OK;
+}
+
+// ---- host-side jump-ahead (no GPU) ----
+int tp_xoshiro_state_at(uint64_t seed, uint64_t jumps128, uint64_t draws, uint64_t state[4]) {
+  if (!state) return TP_ERR_INVALID;
+  xoshiro_seed(seed, state);
+  if (jumps128) {
+    const Tables& t = host_tables();
+    for (int k = 0; k < 64; ++k)
+      if ((jumps128 >> k) & 1) {
+        Gf2Poly p;
+        for (int w = 0; w < 4; ++w) p.w[w] = t.xo_jump[4 * k + w];
+        xoshiro_apply(p, state);
+      }
+  }
+  if (draws) xoshiro_apply(gf2_xpow(draws), state);
+  return TP_OK;
+}
+
+int tp_ranf_state_at(int32_t seed, uint64_t draws, int32_t slots[55], int32_t* index) {
+  if (!slots || !index) return TP_ERR_INVALID;
+  int32_t w[110];
+  ranf_seeded(seed, w);
+  if (!ranf_canonical(w)) return TP_ERR_UNSUPPORTED;
+  for (int i = 0; i < 55; ++i) w[55 + i] = w[i];
+  ranf_reset(w + 55);
+  const uint64_t r = draws / 55, m = draws % 55;
+  ranf_apply(ranf_xpow(55 * r), w, slots);
+  *index = (int32_t)(55 - m);
+  return TP_OK;
+}
+
+}  // extern "C"

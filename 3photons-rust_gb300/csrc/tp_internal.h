@@ -1,0 +1,88 @@
+// tp_internal.h — types shared by the kernels (tp_kernels.cu) and the host
+// code (tp_host.cpp, tp_capi.cpp). Not part of the public ABI.
+#ifndef TP_INTERNAL_H
+#define TP_INTERNAL_H
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/tp_gpu.h"
+
+namespace tp {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double kMinPositive = 2.2250738585072014e-308;  // f64::MIN_POSITIVE
+constexpr int kBatch = TP_BATCH_SIZE;
+constexpr int kDrawsPerEvent = 12;  // default evgen: 3 photons x 4 draws
+constexpr uint64_t kDrawsPerBatch = (uint64_t)kDrawsPerEvent * kBatch;
+
+// Per-run constants of the event path, computed once on the host.
+struct EvConst {
+  double e_total;  // sqrt(s)
+  double half;     // e_total / 2: E of both beams, p_x of the positron
+  double em_x;     // -e_total / 2: p_x of the electron (src/evgen.rs:66-69)
+  double acut, bcut, emin, sincut;
+  // Couplings::new (src/coupling.rs:23-33)
+  double g_a, g_bp, g_bm;
+  // ResultsAccumulator::sigma_contribs (src/resacc.rs:88-100)
+  double sc[5];
+  // Spinor constants of the two beams (src/spinor.rs:37-52): xx = sqrt(E+Z)
+  // and fx = p_x / xx for e- and e+, s(e-, e+) and the amplitude prefactors
+  // c1 = -RAC8 s(e-,e+), c2 = -RAC8 t(e-,e+).
+  double xx_in, fx_em, fx_ep, s01, c1, c2;
+  // factors turning the kernels' unscaled helicity sums into the
+  // reference's m2_sums: (g_a c1)^2, (g_bp c1)^2, (g_bm c1)^2,
+  // -2 g_a g_bp c1^2 (real and imaginary mixed parts)
+  double sc_raw[4];
+  // FP32 copies for the mixed-precision path
+  float f_e_total, f_half, f_em_x, f_acut, f_bcut, f_emin, f_sincut;
+  float f_xx_in, f_fx_em, f_fx_ep, f_c1, f_c2;
+  float f_sc_raw[4];
+  int flags;  // TP_MODE_* bits
+};
+
+// Per-batch outputs in SoA layout: element [c * stride + i]
+struct BatchOut {
+  uint64_t* selected;
+  double* spm2;
+  double* vars;
+  double* sigma;
+  double* variance;
+  uint64_t stride;
+};
+
+struct KParams {
+  EvConst k;
+  uint64_t first_batch;  // absolute index of the launch's first batch
+  uint64_t n_batches;
+  uint64_t num_events;   // events of the whole run
+  int ept;               // xoshiro: events per thread
+  int precision;
+  const void* batch_state;     // xoshiro: 4 x u64 per batch; ranf: 56 x i32
+  const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
+  BatchOut out;
+  unsigned int* err;     // device error word (0 = fine)
+};
+
+// Host-side helpers (tp_host.cpp)
+int make_ev_const(const tp_config& cfg, int flags, EvConst* k);
+double event_weight(double e_total);
+int check_config(const tp_config* cfg);
+
+// Kernel launchers (tp_kernels.cu); `stream` is a cudaStream_t
+int launch_seed_xoshiro(const uint64_t start[4], const uint64_t* d_table, uint64_t first_batch,
+                        uint64_t n_batches, uint64_t* d_out, void* stream);
+int launch_seed_ranf(int jump_per_batch, int32_t seed, const int32_t* d_window,
+                     const uint32_t* d_table, uint64_t first_batch, uint64_t n_batches,
+                     int32_t* d_out, void* stream);
+int launch_events(int rng_kind, const KParams& p, int tpb, void* stream);
+int launch_dump(int rng_kind, const EvConst& k, const uint64_t start[4], const int32_t* d_window,
+                int32_t seed, const uint64_t* d_xo_draw_table, const uint64_t* d_xo_jump_table,
+                const uint32_t* d_ranf_table, uint64_t first_event, uint64_t n,
+                tp_event_dump* d_out, unsigned int* d_err, void* stream);
+
+int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
+
+}  // namespace tp
+
+#endif

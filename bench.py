@@ -1,0 +1,308 @@
+"""Benchmark of the e+e- -> 3 photons event loop on GB300.
+
+Workload (one "step"): the FP64 plain path over 1e9 events = 1e5 batches of
+10 000 at sqrt(s) = 1000 GeV (E_min 5 GeV, |cos| cuts 0.95, alpha =
+1/137.036, M_Z = 91.187, Gamma_Z = 2.490, sin^2 theta_W = 0.2315,
+beta+- = 1), random stream xoshiro256+ seeded with 12345 (the reference's
+`standard-random` stream), draws bit-exact to the reference's sequential
+stream. The inputs are the configuration and the seed; the outputs are the
+13 per-batch sums of every batch.
+
+  value     events/s with the outputs kept on the device (CUDA events on the
+            launching stream; L2 flushed between steps by a 256 MiB write)
+  e2e       events/s through the public C-ABI call with host output arrays
+            (tp_run_batches: launch, run, copy of every batch's sums to host)
+  roofline  the event kernel's FP64 work (canonical per-event count, the
+            transcendental calls weighted by their measured DFMA cost) per
+            second against this GPU's DFMA rate measured here
+  cpu_baseline  the CPU restatement of the reference path on the host cores
+
+`--impl reference` times the reference's CPU path instead (the CPU
+restatement: the Rust reference cannot be built here) on the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD_EVENTS = 1_000_000_000
+SEED = 12345
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+METRIC = "events/s on 1 GB300: FP32-mixed vs FP64 plain at sigma rel.err<=1e-6; grad/fwd time"
+
+
+def workload_config(tp, events):
+    cfg = tp.Configuration.load(os.path.join(ROOT, "tests", "golden", "valeurs_sqrts1000"), echo=False)
+    return cfg.replace(num_events=events)
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + CLOCK_FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[4:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        seen = set()
+        for _, _, flags in rows:
+            for n, f in zip(names, flags[1:]):
+                if f.lower() == "active":
+                    seen.add(n)
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(seen), "samples": len(rows)}
+
+
+def algorithmic_flops_per_event(f_acc, costs):
+    """Canonical FP64 work of one event: 177 + 623 f_acc flops (minimal
+    operation count of the reference formulas), plus per event 3 log, 3
+    sincos, 5 + 3 f_acc sqrt and 2 + 9 f_acc divisions, each weighted by its
+    measured cost in DFMA (2 flops) equivalents."""
+    w = 177.0 + 623.0 * f_acc
+    w += 2.0 * (3 * costs["log"] + 3 * costs["sincos"] + (5 + 3 * f_acc) * costs["sqrt"]
+                + (2 + 9 * f_acc) * costs["div"])
+    return w
+
+
+def cpu_baseline(tp, events_budget_s=3.0):
+    """The CPU restatement (FP64, the same xoshiro stream and physics) on all
+    host cores over a bounded sample of the workload's first batches."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tp_oracle_py
+
+    oracle = tp_oracle_py.Oracle(tp)
+    cfg = workload_config(tp, WORKLOAD_EVENTS)
+    threads = os.cpu_count() or 1
+    kind = tp.rng_flags("xoshiro")
+    nb = max(threads, 8)
+    t0 = time.perf_counter()
+    oracle.run_batches(cfg, 0, nb, kind, SEED, threads)
+    dt = time.perf_counter() - t0
+    nb = max(nb, int(nb * events_budget_s / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    oracle.run_batches(cfg, 0, nb, kind, SEED, threads)
+    dt = time.perf_counter() - t0
+    ev = nb * tp.TP_BATCH_SIZE
+    return {"value": ev / dt, "unit": "events/s", "cores": threads, "kind": "port",
+            "sample": "first %d batches (%d events) of the workload, FP64, %d threads" % (nb, ev, threads)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as graft
+
+    tp = graft.package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tp_oracle_py
+
+    oracle = tp_oracle_py.Oracle(tp)
+    cfg = workload_config(tp, WORKLOAD_EVENTS)
+    threads = os.cpu_count() or 1
+    kind = tp.rng_flags("xoshiro")
+    nb = 4 * threads
+    for _ in range(args.warmup):
+        oracle.run_batches(cfg, 0, nb, kind, SEED, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.run_batches(cfg, 0, nb, kind, SEED, threads)
+        times.append(time.perf_counter() - t0)
+    ev = nb * tp.TP_BATCH_SIZE
+    value = ev * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sqrt(s)=1000 GeV, xoshiro256+ seed 12345, FP64 plain; each step the first "
+                               "%d batches (%d events) of the 1e9-event run" % (nb, ev),
+                   "events_per_step": ev, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                         "sample": "CPU restatement of the reference path (the Rust reference has no toolchain "
+                                   "here), %d threads, %d events per step" % (threads, ev)},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--events", type=int, default=WORKLOAD_EVENTS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import __graft_entry__ as graft
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    tp = graft.package()
+    ctx = tp.Context(local)
+    events = args.events
+    # weak scaling: every rank integrates its own 1e9-event range of one
+    # world * 1e9-event run
+    cfg = workload_config(tp, events * world)
+    nb = (events + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
+    first = rank * nb
+    costs = ctx.probe_fp64()
+
+    dev = torch.device("cuda", local)
+    sel = torch.zeros(nb, dtype=torch.int64, device=dev)
+    f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
+    ptrs = [sel.data_ptr(), f.data_ptr(), f.data_ptr() + 5 * nb * 8, f.data_ptr() + 10 * nb * 8,
+            f.data_ptr() + 11 * nb * 8]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.run_batches_device(cfg, first, nb, ptrs, stream=stream.cuda_stream, rng="xoshiro", seed=SEED)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ctx.profile(True)
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ev_ms, ev_launches, seed_ms, seed_launches = ctx.profile_read()
+    ctx.profile(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) * 1e-3
+    if dist:
+        t = torch.tensor([total_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * events * args.steps / total_s
+
+    selected = int(sel.sum().item())
+    f_acc = selected / events
+    w = algorithmic_flops_per_event(f_acc, costs)
+    launch_ms = ev_ms / max(ev_launches, 1)
+    events_per_launch = events * args.steps / max(ev_launches, 1)
+    achieved = w * events_per_launch / (launch_ms * 1e-3)
+    peak = costs["dfma_flops"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tr = json.load(open(tpath))
+        if "bytes_per_event" in tr:
+            traffic = tr["bytes_per_event"] * events_per_launch
+
+    # end to end through the public API: host output arrays, copies included
+    acc = tp.BatchAccumulators(nb)
+    ctx.run_batches(cfg, first, nb, rng="xoshiro", seed=SEED, out=acc)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.run_batches(cfg, first, nb, rng="xoshiro", seed=SEED, out=acc)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * events * args.steps / e2e_s if world == 1 else events * args.steps / e2e_s * world,
+           "unit": "events/s", "h2d_bytes_per_step": ctypes.sizeof(tp.CConfig),
+           "d2h_bytes_per_step": nb * 13 * 8}
+    sigma = None
+    if rank == 0 and world == 1:
+        sigma = tp.merge_finalize(cfg, acc).sigma
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": sum(step_ms) / len(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "FP64 plain path, sqrt(s)=1000 GeV, xoshiro256+ seed 12345 with jump-ahead, "
+                               "1e9 events = 1e5 batches of 1e4 per GPU",
+                   "events_per_step": events * world, "batches": nb * world, "precision": "fp64",
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": "batch-range shards, no collective"},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "DFMA throughput measured in this run (tp_probe_fp64)",
+                     "kernel": "k_events_xoshiro_fp64", "flops_per_event": w, "f_acc": f_acc,
+                     "dfma_cost": {k: v for k, v in costs.items() if k != "dfma_flops"}},
+        "e2e": e2e,
+        "gpu_launches": int(ev_launches + seed_launches),
+        "kernel_ms": {"events": ev_ms / args.steps, "seed": seed_ms / args.steps},
+        "clocks": clocks.summary(),
+        "result": {"sigma_pb": sigma, "selected": selected},
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(tp)
+    print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,272 @@
+/*
+ * tp_gpu.h — C ABI of the GB300 event kernel for e+e- -> 3 photons.
+ *
+ * This library replaces the per-event loop of 3photons-rust: the scheduler
+ * seam `scheduling::run_simulation(num_events, simulate_events)`
+ * (src/scheduling/mod.rs:31-59) together with its backends
+ * `sequential::run_simulation_impl` (src/scheduling/sequential.rs:15-40) and
+ * `multi_threading::run_simulation_impl` (src/scheduling/multi_threading.rs:16-75),
+ * and the per-batch closure they call (src/main.rs:103-128):
+ * random draws -> RAMBO phase space -> cuts -> spinor products -> helicity
+ * amplitudes -> ResultsAccumulator::integrate (src/resacc.rs:121-129).
+ *
+ * The host keeps the rest of the program: the `valeurs` input
+ * (src/config.rs:57-128), the ordered batch merge (src/resacc.rs:133-139),
+ * finalisation (src/resacc.rs:142-223) and the res.data / stdout writers
+ * (src/output.rs:30-269, src/resfin.rs:66-194).  Those host-side pieces are
+ * exported below as well, so a caller in any language can run the whole
+ * program through this header.
+ *
+ * Conventions (every entry point):
+ *  - plain pointers and sizes only; no CUDA or torch types in signatures;
+ *  - functions return TP_OK (0) on success or a negative TP_ERR_* code and
+ *    never abort; the message of the last failure of a context is returned by
+ *    tp_last_error();
+ *  - one context per host thread; calls are synchronous unless their name
+ *    ends in _async;
+ *  - device memory is owned by the context, host output buffers by the
+ *    caller.
+ */
+#ifndef TP_GPU_H
+#define TP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TP_OK 0
+#define TP_ERR_INVALID (-1)     /* bad argument or configuration            */
+#define TP_ERR_UNSUPPORTED (-2) /* valid request this build does not serve  */
+#define TP_ERR_CUDA (-3)        /* CUDA allocation / launch / copy failure  */
+#define TP_ERR_DEVICE (-4)      /* a kernel raised its device error flag    */
+#define TP_ERR_TIMEOUT (-5)     /* a bounded device wait gave up            */
+#define TP_ERR_NO_DEVICE (-6)   /* no usable CUDA device                    */
+#define TP_ERR_IO (-7)          /* host file input / output failed          */
+
+/* Events per batch: EVENT_BATCH_SIZE (src/scheduling/mod.rs:21). Batch b
+ * holds events [b*TP_BATCH_SIZE, min((b+1)*TP_BATCH_SIZE, num_events)). */
+#define TP_BATCH_SIZE 10000
+
+/* Number of matrix-element contributions A, B+, B-, Re(mixed), Im(mixed)
+ * (src/matelems.rs:21-33). */
+#define TP_NUM_CONTRIB 5
+
+/* ---- random streams ------------------------------------------------------
+ * rng_kind = one TP_RNG_* value, optionally OR-ed with TP_MODE_* flags.
+ *
+ * TP_RNG_RANF: Knuth's subtractive generator (src/random/ranf.rs), seed is
+ *   the i32 ranf seed (reference default 234612947, ranf.rs:31).
+ * TP_RNG_XOSHIRO256P: xoshiro256+ seeded through SplitMix64 from a 64-bit
+ *   seed, uniform = (next_u64 >> 11) * 2^-53 (src/random/standard.rs:21-35;
+ *   reference default seed 12345).
+ *
+ * Without flags the whole run is ONE stream consumed 12 draws per event in
+ * event order, exactly like the reference's sequential and reproducible
+ * multi-threaded schedulers; every batch starts by jump-ahead.
+ * TP_MODE_JUMP_PER_BATCH reproduces `--features
+ * multi-threading,faster-threading`: batch b starts from the seed jumped b
+ * times by RandomGenerator::jump (ranf: reseed with seed+123456*b in i32
+ * wrapping arithmetic, ranf.rs:137-140; xoshiro: b jumps of 2^128 draws,
+ * standard.rs:53-55).
+ * TP_MODE_NO_PHOTON_SORTING reproduces `--features no-photon-sorting`
+ * (src/evgen.rs:109, src/event.rs:96-105). */
+#define TP_RNG_RANF 0
+#define TP_RNG_XOSHIRO256P 1
+#define TP_RNG_KIND_MASK 0xff
+#define TP_MODE_JUMP_PER_BATCH 0x100
+#define TP_MODE_NO_PHOTON_SORTING 0x200
+
+#define TP_RANF_DEFAULT_SEED 234612947ull
+#define TP_XOSHIRO_DEFAULT_SEED 12345ull
+
+/* ---- precision ---------------------------------------------------------- */
+#define TP_PREC_FP64 0       /* FP64 throughout (the reference's default) */
+#define TP_PREC_FP32_MIXED 1 /* FP32 event math, FP64 batch sums, FP64
+                                recheck of events near a cut boundary     */
+
+/* ---- configuration: the 18 items of `valeurs` (src/config.rs:152-198) --- */
+typedef struct tp_config {
+  uint64_t num_events;          /* ITOT: total events of the run; also the
+                                   normalisation of every event weight
+                                   (src/resacc.rs:83-86)                   */
+  double e_total;               /* ETOT, centre-of-mass energy (GeV)      */
+  double beam_photons_cut;      /* ACUT, max |cos(photon, beam)|          */
+  double photon_photon_cut;     /* BCUT, max cos(photon, photon)          */
+  double e_min;                 /* EMIN, min photon energy (GeV)          */
+  double beam_photon_plane_cut; /* SINCUT, min cos(beam, plane normal)    */
+  double alpha;                 /* fine structure constant                */
+  double alpha_z;               /* fine structure constant at the Z peak  */
+  double gev2_to_picobarn;      /* CONVERS                                */
+  double m_z0;                  /* Z mass (GeV)                           */
+  double g_z0;                  /* Z width (GeV)                          */
+  double sin2_weinberg;         /* sin^2(theta_W)                         */
+  double branching_ep_em;       /* BR(Z -> e+e-)                          */
+  double beta_plus;             /* anomalous coupling beta+               */
+  double beta_minus;            /* anomalous coupling beta-               */
+  int32_t num_bins;             /* NBIN (read, unused by the reference)   */
+  int32_t impr;                 /* must be 0 (src/config.rs:265-269)      */
+  int32_t plot;                 /* must be 0 (src/config.rs:260)          */
+  int32_t reserved;             /* keep 0                                 */
+} tp_config;
+
+/* ---- per-batch accumulators: ResultsAccumulator's running sums ---------
+ * (src/resacc.rs:18-34). Structure of arrays, every array n_batches long;
+ * spm2 and vars are contribution-major: element [k * n_batches + b].      */
+typedef struct tp_batch_soa {
+  uint64_t *selected; /* events that passed the cuts                 */
+  double *spm2;       /* [5][n] sum of per-event |M|^2 contributions  */
+  double *vars;       /* [5][n] sum of their squares                  */
+  double *sigma;      /* [n]    sum of event weights                  */
+  double *variance;   /* [n]    sum of squared event weights          */
+} tp_batch_soa;
+
+/* ---- one dumped event (parity checks) ------------------------------------ */
+typedef struct tp_event_dump {
+  double uniforms[12];    /* the 12 draws, in draw order                 */
+  double p_out[3][4];     /* photons after sorting, [photon][X,Y,Z,E]    */
+  int32_t cut;            /* 0 kept; 1 energy, 2 beam, 3 pair, 4 plane   */
+  int32_t reserved;
+  double m2_sums[5];      /* MEsContributions::m2_sums (0 when cut)      */
+} tp_event_dump;
+
+/* ---- final results: FinalResults (src/resfin.rs:26-62) ------------------ */
+typedef struct tp_final_results {
+  uint64_t selected_events;
+  double spm2[2][5]; /* [spin][contribution] */
+  double vars[2][5];
+  double sigma;
+  double prec;
+  double variance;
+  double beta_min;
+  double ss_p, inc_ss_p;
+  double ss_m, inc_ss_m;
+} tp_final_results;
+
+/* ========================================================================
+ * GPU context
+ * ======================================================================== */
+typedef struct tp_ctx tp_ctx;
+
+/* Creates a context on CUDA device `device`. On failure returns NULL and
+ * stores a TP_ERR_* code in *status (if non-NULL). */
+tp_ctx *tp_create(int device, int *status);
+void tp_destroy(tp_ctx *ctx);
+/* Message of the last failing call on `ctx` ("" if none). With ctx == NULL:
+ * the message of the last failing tp_create on this thread. */
+const char *tp_last_error(const tp_ctx *ctx);
+
+/* Runs batches [first_batch, first_batch + n_batches) of a run configured by
+ * `cfg` and writes each batch's accumulators to the caller-owned HOST arrays
+ * of `out`. Replaces run_simulation_impl's loop over batches
+ * (src/scheduling/sequential.rs:15-40) and the per-batch closure
+ * (src/main.rs:103-128); merging in batch order is left to the caller
+ * (tp_merge_finalize below), exactly as ResultsAccumulator::merge does.
+ * first_batch lets a caller resume or shard a run: batch b's random stream
+ * is a pure function of (rng_kind, seed, b). */
+int tp_run_batches(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                   uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+                   int precision, tp_batch_soa *out);
+
+/* Same as tp_run_batches, but `out` holds DEVICE pointers and the work is
+ * queued on `stream` (a cudaStream_t, NULL = the context's stream) without
+ * a host synchronisation. */
+int tp_run_batches_async(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                         uint64_t seed, uint64_t first_batch,
+                         uint64_t n_batches, int precision,
+                         tp_batch_soa *out, void *stream);
+
+/* Recomputes events [first_event, first_event + n) in FP64 and writes one
+ * tp_event_dump per event into the caller's host array (parity checks of
+ * single events against the reference's event loop, src/main.rs:108-124). */
+int tp_dump_events(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                   uint64_t seed, uint64_t first_event, uint64_t n,
+                   tp_event_dump *out);
+
+/* Tuning: events each thread integrates in the xoshiro kernels (default
+ * 40; ceil(10000 / ept) must not exceed 256). No counterpart in the
+ * reference, whose batches run on one CPU thread each. */
+int tp_set_events_per_thread(tp_ctx *ctx, int ept);
+
+/* ---- measurement (no counterpart in the reference, which only measures
+ * its wall-clock time, src/main.rs:85,138) ------------------------------
+ * tp_profile(ctx, 1) starts recording a CUDA event pair around every kernel
+ * the context launches; tp_profile_read() waits for them and returns the
+ * summed device time (ms) and launch count of the event kernels and of the
+ * stream-seeding kernels, then clears the record. tp_profile(ctx, 0) stops.
+ * tp_probe_fp64 measures this device's FP64 rates: out[0] = DFMA
+ * throughput in flop/s (an FMA counts 2), out[1..4] = the cost of one
+ * log, sincos, sqrt and division in DFMA-equivalents. */
+int tp_profile(tp_ctx *ctx, int enable);
+int tp_profile_read(tp_ctx *ctx, double *event_ms, uint64_t *event_launches,
+                    double *seed_ms, uint64_t *seed_launches);
+int tp_probe_fp64(tp_ctx *ctx, double out[5]);
+
+/* ---- host-side jump-ahead (no GPU) ----------------------------------------
+ * State of a stream after `draws` draws, computed by polynomial jump-ahead:
+ * checkpoint/resume and sharding need no stepping. xoshiro: seed_from_u64
+ * (src/random/standard.rs:21-25), then `jumps128` RandomGenerator::jump()
+ * calls (standard.rs:53-55), then `draws` draws. ranf: seeded_new
+ * (src/random/ranf.rs:36-66) then `draws` draws: slots 1..55 and the
+ * remaining draws of the current block (`index`). Returns
+ * TP_ERR_UNSUPPORTED when the ranf seed leaves its state outside [0, 1e9). */
+int tp_xoshiro_state_at(uint64_t seed, uint64_t jumps128, uint64_t draws,
+                        uint64_t state[4]);
+int tp_ranf_state_at(int32_t seed, uint64_t draws, int32_t slots[55],
+                     int32_t *index);
+
+/* ========================================================================
+ * Host side kept from the reference (no GPU needed)
+ * ======================================================================== */
+
+/* Parses a `valeurs` file: the first whitespace-separated token of every
+ * non-blank line, 18 items (Configuration::load, src/config.rs:57-128),
+ * and applies its checks (num_events > 0, plot and impr false). If `echo`
+ * is non-NULL, the configuration echo of src/config.rs:131-155 is written
+ * there (NUL-terminated, truncated to echo_len). */
+int tp_config_load(const char *path, tp_config *out, char *echo,
+                   size_t echo_len);
+
+/* The two values the reference computes once per run on the host:
+ * EventGenerator::event_weight (src/evgen.rs:40-77) and the couplings
+ * (src/coupling.rs:23-33). */
+int tp_event_weight(double e_total, double *weight);
+
+/* Merges n_batches per-batch accumulators in batch order
+ * (ResultsAccumulator::merge, src/resacc.rs:133-139) and finalises them
+ * (ResultsAccumulator::finalize, src/resacc.rs:142-223). */
+int tp_merge_finalize(const tp_config *cfg, const tp_batch_soa *batches,
+                      uint64_t n_batches, tp_final_results *res);
+
+/* res.data text (src/output.rs:62-142) into `buf` (NUL-terminated,
+ * truncated). Returns the full length needed, or a negative TP_ERR_* code. */
+int tp_format_res_data(const tp_config *cfg, const tp_final_results *res,
+                       char *buf, size_t buf_len);
+
+/* Writes res.data exactly as src/output.rs:62-142 does. */
+int tp_write_res_data(const tp_config *cfg, const tp_final_results *res,
+                      const char *path);
+
+/* The two other files of a run (src/output.rs:35-60, 144-173): res.times
+ * (UTC timestamp and elapsed seconds) and one appended record in pil.mc.
+ * `timestamp` is the "dd-Mon-yy HH:MM:SS" stamp of the run's end; NULL
+ * takes the current UTC time. */
+int tp_write_res_times(const tp_config *cfg, double elapsed_seconds,
+                       const char *timestamp, const char *path);
+int tp_append_pil_mc(const tp_config *cfg, const tp_final_results *res,
+                     const char *timestamp, const char *path);
+
+/* Formats the physics printout of FinalResults::eric and ::fawzi
+ * (src/resfin.rs:66-194) into `buf` (NUL-terminated, truncated). Returns
+ * the full length needed, or a negative TP_ERR_* code. */
+int tp_format_report(const tp_config *cfg, const tp_final_results *res,
+                     char *buf, size_t buf_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TP_GPU_H */

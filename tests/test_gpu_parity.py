@@ -1,0 +1,157 @@
+"""GPU event loop (through the C ABI) against the CPU restatement and the
+reference's goldens.
+
+Integer results (uniforms, cut decisions, selected-event counts) must be
+bit-exact. Floating-point sums: per batch within 1e-12 relative (the GPU
+sums a batch in a tree, the reference left to right; measured differences
+are ~1e-15). Momenta: within 64 ulps (CUDA's log/sin/cos and glibc's may
+differ in their last bit)."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from numdiff import compare
+
+pytestmark = pytest.mark.gpu
+
+MODES = [
+    ("ranf", False, True),
+    ("xoshiro", False, True),
+    ("ranf", True, True),
+    ("xoshiro", True, True),
+    ("ranf", False, False),
+    ("xoshiro", False, False),
+]
+IDS = ["ranf", "xoshiro", "ranf-jump", "xoshiro-jump", "ranf-nosort", "xoshiro-nosort"]
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))) if a.size else 0.0
+
+
+def assert_batches_close(gpu, ref, tol=1e-12):
+    assert np.array_equal(gpu.selected, ref.selected)
+    for name in ("spm2", "vars", "sigma", "variance"):
+        g, r = getattr(gpu, name), getattr(ref, name)
+        if name in ("spm2",):
+            # Re/Im(mixed) sums cancel: compare them on the scale of the A row
+            scale = np.maximum(np.abs(r), np.abs(ref.spm2[0])[None, :])
+            err = float(np.max(np.abs(g - r) / np.maximum(scale, 1e-300)))
+        else:
+            err = rel(g, r)
+        assert err < tol, (name, err)
+
+
+@pytest.mark.parametrize("rng,jump,sort", MODES, ids=IDS)
+def test_batches_match_restatement(tp, oracle, ctx, cfg_valeurs, rng, jump, sort):
+    cfg = cfg_valeurs.replace(num_events=123_456)  # 13 batches, the last one partial
+    nb = cfg.num_batches
+    gpu = ctx.run_batches(cfg, 0, nb, rng=rng, jump_per_batch=jump, sorting=sort)
+    ref = oracle.run_batches(cfg, 0, nb, tp.rng_flags(rng, jump, sort), tp.default_seed(rng))
+    assert_batches_close(gpu, ref)
+    assert gpu.selected[-1] < gpu.selected[0]  # partial batch
+
+
+@pytest.mark.parametrize("rng,jump", [("ranf", False), ("xoshiro", False), ("xoshiro", True), ("ranf", True)])
+def test_resume_at_any_batch(tp, oracle, ctx, cfg_valeurs, rng, jump):
+    # batch b's stream is a pure function of b: resuming at batch 977 of a
+    # 1e7 run gives the same accumulators as the uninterrupted run
+    cfg = cfg_valeurs
+    gpu = ctx.run_batches(cfg, 977, 3, rng=rng, jump_per_batch=jump)
+    ref = oracle.run_batches(cfg, 977, 3, tp.rng_flags(rng, jump), tp.default_seed(rng))
+    assert_batches_close(gpu, ref)
+
+
+@pytest.mark.parametrize("n", [1, 7, 9999, 10000, 10001, 20000])
+def test_small_and_ragged_sizes(tp, oracle, ctx, cfg_valeurs, n):
+    cfg = cfg_valeurs.replace(num_events=n)
+    for rng in ("ranf", "xoshiro"):
+        gpu = ctx.run_batches(cfg, 0, cfg.num_batches, rng=rng)
+        ref = oracle.run_batches(cfg, 0, cfg.num_batches, tp.rng_flags(rng), tp.default_seed(rng))
+        assert_batches_close(gpu, ref)
+
+
+def test_batches_beyond_the_run_are_empty(tp, ctx, cfg_valeurs):
+    cfg = cfg_valeurs.replace(num_events=25_000)
+    gpu = ctx.run_batches(cfg, 0, 5, rng="xoshiro")
+    assert gpu.selected[3] == 0 and gpu.selected[4] == 0 and gpu.sigma[4] == 0.0
+
+
+@pytest.mark.parametrize("rng,jump,sort", MODES[:4], ids=IDS[:4])
+def test_event_dumps(tp, oracle, ctx, cfg_valeurs, rng, jump, sort):
+    first, n = 9_990_000 - 37, 20_000  # crosses a batch boundary
+    g = ctx.dump_events(cfg_valeurs, first, n, rng=rng, jump_per_batch=jump, sorting=sort)
+    r = oracle.dump_events(cfg_valeurs, tp.rng_flags(rng, jump, sort), tp.default_seed(rng), first, n)
+    assert np.array_equal(g["uniforms"], r["uniforms"])  # bit-exact draws
+    assert np.array_equal(g["cut"], r["cut"])  # identical cut decisions
+    # momenta within 1e-12 of sqrt(s): CUDA's and glibc's log/sin/cos may
+    # differ in their last bit, which the conformal map amplifies when the
+    # three raw photons are nearly collinear (R^2 = R_E^2 - |R|^2 cancels)
+    d = np.abs(g["p_out"] - r["p_out"])
+    assert float(d.max()) <= 1e-12 * cfg_valeurs.e_total, float(d.max())
+    ulp = np.spacing(np.abs(r["p_out"]).max(axis=2, keepdims=True))
+    assert np.mean(d <= 8 * ulp) > 0.999
+    kept = r["cut"] == 0
+    m_g, m_r = g["m2_sums"][kept], r["m2_sums"][kept]
+    scale = np.maximum(np.abs(m_r), np.abs(m_r[:, :1]))
+    assert np.max(np.abs(m_g - m_r) / scale) < 1e-12
+
+
+@pytest.mark.parametrize("features,rng,jump,sort", [
+    ("", "ranf", False, True),
+    ("standard-random", "xoshiro", False, True),
+    ("multi-threading,faster-threading", "ranf", True, True),
+    ("standard-random,multi-threading,faster-threading", "xoshiro", True, True),
+    ("no-photon-sorting", "ranf", False, False),
+])
+def test_golden_run(tp, ctx, cfg_valeurs, features, rng, jump, sort):
+    res = tp.run_simulation(cfg_valeurs, rng=rng, jump_per_batch=jump, sorting=sort, ctx=ctx)
+    gold = golden("res.data", features)
+    # the selected-event count is an exact check of every cut decision
+    assert res.res_data().splitlines()[1] == gold.splitlines()[1]
+    assert compare(res.res_data(), gold, rel_tol=1e-12) == []
+    assert compare(res.report(), golden("stdout.log", features).split("IBegin", 1)[1], rel_tol=1e-12) == []
+
+
+def test_deterministic(ctx, cfg_valeurs):
+    cfg = cfg_valeurs.replace(num_events=200_000)
+    a = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro")
+    b = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro")
+    assert a.as_array().tobytes() == b.as_array().tobytes()
+
+
+@pytest.mark.parametrize("ept", [40, 41, 64, 100, 333, 10000])
+def test_events_per_thread_invariance(tp, oracle, cfg_valeurs, ept):
+    cfg = cfg_valeurs.replace(num_events=30_000)
+    with tp.Context(0) as c:
+        c.set_events_per_thread(ept)
+        gpu = c.run_batches(cfg, 0, 3, rng="xoshiro")
+    ref = oracle.run_batches(cfg, 0, 3, tp.rng_flags("xoshiro"), tp.XOSHIRO_DEFAULT_SEED)
+    assert_batches_close(gpu, ref)
+
+
+def test_sqrts1000_configuration(tp, oracle, ctx, cfg_sqrts1000):
+    cfg = cfg_sqrts1000
+    nb = cfg.num_batches
+    gpu = ctx.run_batches(cfg, 0, nb, rng="ranf")
+    ref = oracle.run_batches(cfg, 0, nb, tp.rng_flags("ranf"), tp.RANF_DEFAULT_SEED)
+    assert_batches_close(gpu, ref)
+    a = tp.merge_finalize(cfg, gpu)
+    b = tp.merge_finalize(cfg, ref)
+    assert compare(a.res_data(), b.res_data(), rel_tol=1e-12) == []
+
+
+def test_invalid_arguments(tp, ctx, cfg_valeurs):
+    with pytest.raises(tp.TPError) as e:
+        ctx.run_batches(cfg_valeurs.replace(num_events=0), 0, 1)
+    assert e.value.code == tp.TP_ERR_INVALID
+    with pytest.raises(tp.TPError) as e:
+        ctx.run_batches(cfg_valeurs, 0, 1, rng="ranf", seed=2**40)
+    assert e.value.code == tp.TP_ERR_INVALID
+    with pytest.raises(tp.TPError) as e:
+        ctx.set_events_per_thread(0)
+    with pytest.raises(tp.TPError) as e:
+        ctx.set_events_per_thread(39)  # 257 threads: beyond one CTA
+    # the context stays usable after errors
+    ctx.run_batches(cfg_valeurs.replace(num_events=1000), 0, 1, rng="xoshiro")
