@@ -149,6 +149,7 @@ def library():
         "tp_profile": (i32, [vp, i32]),
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
+        "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
         "tp_xoshiro_state_at": (i32, [u64, u64, u64, P(ctypes.c_uint64)]),
         "tp_ranf_state_at": (i32, [ctypes.c_int32, u64, P(ctypes.c_int32), P(ctypes.c_int32)]),
         "tp_config_load": (i32, [ctypes.c_char_p, P(CConfig), ctypes.c_char_p, ctypes.c_size_t]),
@@ -373,6 +374,12 @@ class Context:
         out = (ctypes.c_double * 5)()
         self.check(library().tp_probe_fp64(self.h, out))
         return {"dfma_flops": out[0], "log": out[1], "sincos": out[2], "sqrt": out[3], "div": out[4]}
+
+    def recheck_count(self, reset=True):
+        """Events the FP32-mixed path settled with its FP64 recheck."""
+        n = ctypes.c_uint64()
+        self.check(library().tp_recheck_count(self.h, ctypes.byref(n), 1 if reset else 0))
+        return n.value
 
     def run_batches(self, cfg, first_batch, n_batches, rng="ranf", seed=None, jump_per_batch=False, sorting=True,
                     precision=TP_PREC_FP64, out=None):

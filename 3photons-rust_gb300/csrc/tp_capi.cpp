@@ -77,6 +77,7 @@ struct tp_ctx {
   void* d_dump = nullptr;
   size_t dump_bytes = 0;
   unsigned int* d_err = nullptr;
+  unsigned long long* d_recheck = nullptr;  // FP32-mixed events settled in FP64
   // optional CUDA-event timing of every kernel launch (tp_profile)
   int prof = 0;
   std::vector<cudaEvent_t> ev_pool;
@@ -172,8 +173,8 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   if (n_batches == 0) return TP_OK;
   if (first_batch > (1ull << 46) || n_batches > (1ull << 46))
     return c->fail(TP_ERR_INVALID, "batch range too large");
-  if (precision != TP_PREC_FP64)
-    return c->fail(TP_ERR_UNSUPPORTED, "precision not available in this build");
+  if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
+    return c->fail(TP_ERR_INVALID, "unknown precision");
   const int kind = rng_kind & TP_RNG_KIND_MASK;
   const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
   KParams kp{};
@@ -181,6 +182,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   kp.num_events = cfg->num_events;
   kp.precision = precision;
   kp.err = c->d_err;
+  kp.recheck_count = c->d_recheck;
   kp.ept = c->ept;
   if (kind == TP_RNG_XOSHIRO256P) {
     if (int st = ensure_thread_poly(c, c->ept)) return st;
@@ -262,6 +264,7 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_thread_poly, kTpb * 32, "tables");
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
+  alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
   alloc(&c->d_state, kChunk * 56 * 4, "batch states");
   (void)dummy;
   (void)p;
@@ -270,6 +273,7 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_draw, t.xo_draw.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), 64 * 55 * 4, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
+  if (!st) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof(unsigned long long)), "recheck counter");
   if (st) {
     g_create_error = c->err;
     if (status) *status = st;
@@ -285,7 +289,7 @@ void tp_destroy(tp_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly,
-                  c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err};
+                  c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -371,6 +375,17 @@ int tp_set_events_per_thread(tp_ctx* c, int ept) {
   if (ept <= 0 || (TP_BATCH_SIZE + ept - 1) / ept > kTpb) return c->fail(TP_ERR_INVALID, "events per thread out of range");
   c->ept = ept;
   return TP_OK;
+}
+
+int tp_recheck_count(tp_ctx* c, uint64_t* count, int reset) {
+  if (!c || !count) return TP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  unsigned long long h = 0;
+  int st = c->cuda(cudaMemcpyAsync(&h, c->d_recheck, sizeof h, cudaMemcpyDeviceToHost, c->stream), "recheck counter");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "recheck counter");
+  if (!st && reset) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof h), "recheck counter");
+  if (!st) *count = h;
+  return st;
 }
 
 int tp_profile(tp_ctx* c, int enable) {

@@ -266,6 +266,7 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   k.f_c1 = (float)k.c1;
   k.f_c2 = (float)k.c2;
   for (int c = 0; c < 4; ++c) k.f_sc_raw[c] = (float)k.sc_raw[c];
+  for (int c = 0; c < 5; ++c) k.f_sc[c] = (float)k.sc[c];
   k.flags = flags;
   *out = k;
   return TP_OK;

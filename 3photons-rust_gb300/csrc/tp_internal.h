@@ -38,6 +38,7 @@ struct EvConst {
   float f_e_total, f_half, f_em_x, f_acut, f_bcut, f_emin, f_sincut;
   float f_xx_in, f_fx_em, f_fx_ep, f_c1, f_c2;
   float f_sc_raw[4];
+  float f_sc[5];
   int flags;  // TP_MODE_* bits
 };
 
@@ -62,6 +63,7 @@ struct KParams {
   const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
   BatchOut out;
   unsigned int* err;     // device error word (0 = fine)
+  unsigned long long* recheck_count;  // FP32-mixed: events decided by the FP64 recheck
 };
 
 // Host-side helpers (tp_host.cpp)

@@ -134,6 +134,85 @@ def cpu_baseline(tp, events_budget_s=3.0):
             "sample": "first %d batches (%d events) of the workload, FP64, %d threads" % (nb, ev, threads)}
 
 
+RES_FIELDS = ("sigma", "prec", "beta_min", "ss_p", "inc_ss_p", "ss_m", "inc_ss_m")
+
+
+def precision_report(r32, r64):
+    """Relative error of every res.data quantity of the FP32-mixed path
+    against the FP64 path on the same events, next to its statistical error.
+    Contributions that are statistically zero are measured on the scale of
+    the A contribution of the same spin."""
+    out = {}
+    for f in RES_FIELDS:
+        a, b = getattr(r32, f), getattr(r64, f)
+        out[f] = abs(a - b) / abs(b) if b else abs(a - b)
+    names = ["A", "B+", "B-", "Re_mixed", "Im_mixed"]
+    for s in range(2):
+        for c in range(5):
+            a, b = r32.spm2[s, c], r64.spm2[s, c]
+            scale = abs(b) if c < 3 else abs(r64.spm2[s, 0])
+            out["spm2_%d_%s" % (s + 1, names[c])] = abs(a - b) / scale if scale else abs(a - b)
+    stat = {"sigma": r64.prec}
+    for s in range(2):
+        for c in range(3):
+            stat["spm2_%d_%s" % (s + 1, names[c])] = float(r64.vars[s, c])
+    return out, stat
+
+
+def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value, acc64, cfg64, first, nb64):
+    """The precision form: FP32 phase space, spinors and amplitudes, FP64 batch
+    sums, FP64 recheck of events near a cut boundary, on 1e10 events per GPU
+    (1e6 batches). Its accuracy is measured on the FP64 leg's 1e9 events."""
+    ev32 = 10 * events
+    nb = (ev32 + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
+    cfg = workload_config(tp, ev32 * world)
+    first32 = rank * nb
+    sel = torch.zeros(nb, dtype=torch.int64, device=dev)
+    f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
+    ptrs = [sel.data_ptr(), f.data_ptr(), f.data_ptr() + 5 * nb * 8, f.data_ptr() + 10 * nb * 8,
+            f.data_ptr() + 11 * nb * 8]
+
+    def step():
+        ctx.run_batches_device(cfg, first32, nb, ptrs, stream=stream.cuda_stream, rng="xoshiro", seed=SEED,
+                               precision=tp.TP_PREC_FP32_MIXED)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step()
+    torch.cuda.synchronize()
+    ctx.recheck_count(reset=True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ctx.profile(True)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    ev_ms, ev_launches, seed_ms, seed_launches = ctx.profile_read()
+    ctx.profile(False)
+    rechecked = ctx.recheck_count(reset=True)
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    value = world * ev32 * args.steps / (sum(step_ms) * 1e-3)
+    out = {"value": value, "unit": "events/s", "events_per_step": ev32 * world, "ms_per_step": sum(step_ms) / len(step_ms),
+           "kernel": "k_events_xoshiro_fp32", "kernel_ms": ev_ms / args.steps,
+           "gpu_launches": int(ev_launches + seed_launches), "ratio_vs_fp64": None,
+           "rechecked_fraction": rechecked / (ev32 * args.steps)}
+    if fp64_value:
+        out["ratio_vs_fp64"] = value / fp64_value
+    else:
+        del out["ratio_vs_fp64"]
+    if world == 1 and acc64 is not None:
+        acc32 = ctx.run_batches(cfg64, first, nb64, rng="xoshiro", seed=SEED, precision=tp.TP_PREC_FP32_MIXED)
+        r32 = tp.merge_finalize(cfg64, acc32)
+        r64 = tp.merge_finalize(cfg64, acc64)
+        err, stat = precision_report(r32, r64)
+        out["accuracy_vs_fp64"] = {"events": events, "selected_equal": bool(r32.selected_events == r64.selected_events),
+                                   "max_rel_err": max(err.values()), "rel_err": err, "stat_rel_err": stat}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -181,6 +260,8 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--events", type=int, default=WORKLOAD_EVENTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", choices=["fp64", "fp32"], default=None,
+                    help="time one leg only (no e2e, no CPU baseline): for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -206,6 +287,12 @@ def main():
     cfg = workload_config(tp, events * world)
     nb = (events + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
     first = rank * nb
+    if args.only == "fp32":
+        out = fp32_leg(tp, ctx, torch, torch.device("cuda", local), torch.cuda.Stream(torch.device("cuda", local)),
+                       args, events // 10, world, rank, None, None, None, 0, 0)
+        if rank == 0:
+            print(json.dumps(out))
+        return
     costs = ctx.probe_fp64()
 
     dev = torch.device("cuda", local)
@@ -214,7 +301,7 @@ def main():
     ptrs = [sel.data_ptr(), f.data_ptr(), f.data_ptr() + 5 * nb * 8, f.data_ptr() + 10 * nb * 8,
             f.data_ptr() + 11 * nb * 8]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # a named stream: the library launches on it
 
     def step():
         ctx.run_batches_device(cfg, first, nb, ptrs, stream=stream.cuda_stream, rng="xoshiro", seed=SEED)
@@ -229,17 +316,23 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
         ctx.profile(True)
-        for k in range(args.steps):
-            flush.zero_()
-            starts[k].record(stream)
-            step()
-            ends[k].record(stream)
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                step()
+                ends[k].record(stream)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
     ev_ms, ev_launches, seed_ms, seed_launches = ctx.profile_read()
     ctx.profile(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    if args.only == "fp64":
+        if rank == 0:
+            print(json.dumps({"leg": "fp64", "events": events, "ms_per_step": sum(step_ms) / len(step_ms),
+                              "events_per_s": events * len(step_ms) / (sum(step_ms) * 1e-3)}))
+        return
     total_s = sum(step_ms) * 1e-3
     if dist:
         t = torch.tensor([total_s], device=dev)
@@ -275,6 +368,8 @@ def main():
     if rank == 0 and world == 1:
         sigma = tp.merge_finalize(cfg, acc).sigma
 
+    fp32 = fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, value, acc, cfg, first, nb)
+
     if rank != 0:
         return
     line = {
@@ -295,6 +390,7 @@ def main():
         "kernel_ms": {"events": ev_ms / args.steps, "seed": seed_ms / args.steps},
         "clocks": clocks.summary(),
         "result": {"sigma_pb": sigma, "selected": selected},
+        "fp32_mixed": fp32,
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(tp)

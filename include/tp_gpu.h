@@ -205,6 +205,12 @@ int tp_profile_read(tp_ctx *ctx, double *event_ms, uint64_t *event_launches,
                     double *seed_ms, uint64_t *seed_launches);
 int tp_probe_fp64(tp_ctx *ctx, double out[5]);
 
+/* Number of events the FP32-mixed path handed to its FP64 recheck (events
+ * whose cut decision lay within the FP32 error bound) since the context was
+ * created or the counter last reset (reset != 0 clears it after reading).
+ * The reference has no mixed-precision path. */
+int tp_recheck_count(tp_ctx *ctx, uint64_t *count, int reset);
+
 /* ---- host-side jump-ahead (no GPU) ----------------------------------------
  * State of a stream after `draws` draws, computed by polynomial jump-ahead:
  * checkpoint/resume and sharding need no stepping. xoshiro: seed_from_u64

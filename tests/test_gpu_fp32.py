@@ -1,0 +1,54 @@
+"""FP32-mixed path against the FP64 path on the same events.
+
+The cut decisions are certified: an event whose FP32 cut comparison lies
+within the FP32 error bound is settled by an FP64 recheck, so the
+selected-event counts must equal the FP64 path's exactly. The per-batch sums
+carry FP32 rounding (about 1e-7 per event, averaging out); res.data
+quantities must agree with the FP64 path within 1e-6 relative, except those
+that are statistically zero (Re and Im of the mixed term at sqrt(s) = M_Z),
+which are compared on the scale of the A contribution."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("rng,jump", [("xoshiro", False), ("ranf", False), ("xoshiro", True), ("ranf", True)])
+def test_fp32_decisions_match_fp64(tp, ctx, cfg_valeurs, rng, jump):
+    cfg = cfg_valeurs.replace(num_events=1_000_000)
+    nb = cfg.num_batches
+    ctx.recheck_count(reset=True)
+    f32 = ctx.run_batches(cfg, 0, nb, rng=rng, jump_per_batch=jump, precision=tp.TP_PREC_FP32_MIXED)
+    rechecked = ctx.recheck_count(reset=True)
+    f64 = ctx.run_batches(cfg, 0, nb, rng=rng, jump_per_batch=jump)
+    assert np.array_equal(f32.selected, f64.selected)
+    assert 0 < rechecked < 1e-3 * cfg.num_events
+    # per-batch sums: FP32 events, FP64 batch sums
+    for name in ("sigma", "variance"):
+        a, b = getattr(f32, name), getattr(f64, name)
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-5, name
+    for c in (0, 1, 2):
+        assert np.max(np.abs(f32.spm2[c] - f64.spm2[c]) / np.abs(f64.spm2[c])) < 1e-5
+        assert np.max(np.abs(f32.vars[c] - f64.vars[c]) / np.abs(f64.vars[c])) < 1e-5
+    for c in (3, 4):
+        assert np.max(np.abs(f32.spm2[c] - f64.spm2[c]) / np.abs(f64.spm2[0])) < 1e-5
+
+
+@pytest.mark.parametrize("cfg_name", ["cfg_valeurs", "cfg_sqrts1000"])
+def test_fp32_res_data_within_1e6(tp, ctx, request, cfg_name):
+    cfg = request.getfixturevalue(cfg_name)
+    cfg = cfg.replace(num_events=min(cfg.num_events, 10_000_000))
+    r32 = tp.run_simulation(cfg, rng="xoshiro", precision=tp.TP_PREC_FP32_MIXED, ctx=ctx)
+    r64 = tp.run_simulation(cfg, rng="xoshiro", ctx=ctx)
+    assert r32.selected_events == r64.selected_events
+    for f in ("sigma", "beta_min", "ss_p", "ss_m", "prec", "inc_ss_p", "inc_ss_m"):
+        a, b = getattr(r32, f), getattr(r64, f)
+        assert abs(a - b) <= 1e-6 * abs(b), (f, a, b)
+    scale = np.abs(r64.spm2[:, :1])
+    for s in range(2):
+        for c in range(5):
+            a, b = r32.spm2[s, c], r64.spm2[s, c]
+            if c < 3:
+                assert abs(a - b) <= 1e-6 * abs(b), (s, c, a, b)
+            else:
+                assert abs(a - b) <= 1e-6 * scale[s, 0], (s, c, a, b)
