@@ -120,6 +120,21 @@ class CFinalResults(ctypes.Structure):
     ]
 
 
+class CBinning(ctypes.Structure):
+    _fields_ = [
+        ("n_emax", ctypes.c_int32),
+        ("n_cos", ctypes.c_int32),
+        ("emax_lo", ctypes.c_double),
+        ("emax_hi", ctypes.c_double),
+        ("cos_lo", ctypes.c_double),
+        ("cos_hi", ctypes.c_double),
+    ]
+
+
+BIN_STRIDE = 8  # raw sums R_0..R_4, events, sum w, sum w^2
+THETA = ("beta_plus", "beta_minus", "m_z0", "g_z0")
+
+
 DUMP_DTYPE = np.dtype(
     [("uniforms", "<f8", (12,)), ("p_out", "<f8", (3, 4)), ("cut", "<i4"), ("reserved", "<i4"), ("m2_sums", "<f8", (5,))]
 )
@@ -145,11 +160,16 @@ def library():
         "tp_run_batches": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa)]),
         "tp_run_batches_async": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
         "tp_dump_events": (i32, [vp, P(CConfig), i32, u64, u64, u64, vp]),
+        "tp_dump_events_prec": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, vp]),
         "tp_set_events_per_thread": (i32, [vp, i32]),
         "tp_profile": (i32, [vp, i32]),
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
         "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
+        "tp_binned_forward": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp]),
+        "tp_binned_adjoint": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp,
+                                    P(ctypes.c_double), P(ctypes.c_double)]),
+        "tp_coupling_factors": (i32, [P(CConfig), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
         "tp_xoshiro_state_at": (i32, [u64, u64, u64, P(ctypes.c_uint64)]),
         "tp_ranf_state_at": (i32, [ctypes.c_int32, u64, P(ctypes.c_int32), P(ctypes.c_int32)]),
         "tp_config_load": (i32, [ctypes.c_char_p, P(CConfig), ctypes.c_char_p, ctypes.c_size_t]),
@@ -401,12 +421,109 @@ class Context:
                                                   seed, first_batch, n_batches, precision, ctypes.byref(soa),
                                                   ctypes.c_void_p(stream)))
 
-    def dump_events(self, cfg, first_event, n, rng="ranf", seed=None, jump_per_batch=False, sorting=True):
+    def binned_forward(self, cfg, first_batch, n_batches, binning, seed=XOSHIRO_DEFAULT_SEED,
+                       precision=TP_PREC_FP64, jump_per_batch=False):
+        """Per-bin sums [n_bins, 8]: raw R_0..R_4, events, sum w, sum w^2."""
+        nb = binning.n_emax * binning.n_cos
+        out = np.zeros((nb, BIN_STRIDE), np.float64)
+        self.check(library().tp_binned_forward(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch),
+                                               seed, first_batch, n_batches, precision, ctypes.byref(binning),
+                                               ctypes.c_void_p(out.ctypes.data)))
+        return out
+
+    def binned_adjoint(self, cfg, first_batch, n_batches, binning, bin_weight, seed=XOSHIRO_DEFAULT_SEED,
+                       precision=TP_PREC_FP64, jump_per_batch=False):
+        """(g, s): g_c = sum_e r[bin(e)] raw_c,e, s_c = sum_e raw_c,e."""
+        w = np.ascontiguousarray(bin_weight, np.float64)
+        g = (ctypes.c_double * 5)()
+        sm = (ctypes.c_double * 5)()
+        self.check(library().tp_binned_adjoint(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch),
+                                               seed, first_batch, n_batches, precision, ctypes.byref(binning),
+                                               ctypes.c_void_p(w.ctypes.data), g, sm))
+        return np.array(g[:]), np.array(sm[:])
+
+    def dump_events(self, cfg, first_event, n, rng="ranf", seed=None, jump_per_batch=False, sorting=True,
+                    precision=TP_PREC_FP64):
         seed = default_seed(rng) if seed is None else seed
         out = np.zeros(n, DUMP_DTYPE)
-        self.check(library().tp_dump_events(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
-                                            seed, first_event, n, ctypes.c_void_p(out.ctypes.data)))
+        self.check(library().tp_dump_events_prec(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+                                                 seed, first_event, n, precision, ctypes.c_void_p(out.ctypes.data)))
         return out
+
+
+def coupling_factors(cfg):
+    """(K[5], dK[5, 4], flux): K_c(theta), dK_c/d(beta+, beta-, M_Z, Gamma_Z)."""
+    k = (ctypes.c_double * 5)()
+    dk = (ctypes.c_double * 20)()
+    flux = ctypes.c_double()
+    _check(library().tp_coupling_factors(ctypes.byref(cfg.c), k, dk, ctypes.byref(flux)))
+    return np.array(k[:]), np.array(dk[:]).reshape(5, 4), flux.value
+
+
+def binning(n_emax=20, n_cos=20, emax=(0.0, 0.0), cos=(0.0, 0.0)):
+    """E of the most energetic photon x cos(it, e- beam); (0, 0) ranges mean
+    [sqrt(s)/3, sqrt(s)/2] and [-ACUT, ACUT]."""
+    return CBinning(n_emax, n_cos, emax[0], emax[1], cos[0], cos[1])
+
+
+class BinnedGaussianLikelihood:
+    """ln L(theta) = -1/2 sum_b (mu_b(theta) - d_b)^2 / v_b, the binned
+    Gaussian log-likelihood of a model run against pseudo-data.
+
+    mu_b(theta) = flux sum_{e in b} w_e(theta) over the model's events; the
+    data histogram d_b (and its variance v_b = flux^2 sum w^2, from the data
+    run) comes from another run, e.g. at other couplings and another seed.
+    theta = (beta+, beta-, M_Z, Gamma_Z). Events do not depend on theta
+    (only their weights do), so every evaluation reuses the model's seed.
+
+    value(theta): forward pass (events recomputed on the GPU).
+    gradient(theta): forward pass, then the adjoint pass with r_b =
+    d lnL/d mu_b; returns d lnL/dtheta and d sigma/dtheta.
+    analytic_gradient(theta): the same derivatives from the forward pass's
+    per-bin raw sums R_bc (mu_b = flux sum_c R_bc K_c(theta)), the reference
+    for the adjoint.
+    """
+
+    def __init__(self, ctx, cfg, seed, n_batches, data_hist, data_cfg, bins, precision=TP_PREC_FP64):
+        self.ctx, self.cfg, self.seed, self.n_batches = ctx, cfg, seed, n_batches
+        self.bins, self.precision = bins, precision
+        _, _, flux_d = coupling_factors(data_cfg)
+        self.data = flux_d * data_hist[:, 6]
+        var = flux_d ** 2 * data_hist[:, 7]
+        self.var = np.where(var > 0, var, max(var.max(), 1e-300) * 1e-12 + 1e-300)
+        self.last_hist = None
+
+    def theta_cfg(self, theta):
+        return self.cfg.replace(**dict(zip(THETA, [float(t) for t in theta])))
+
+    def _mu(self, hist, cfg):
+        k, dk, flux = coupling_factors(cfg)
+        return flux * hist[:, :5] @ k, k, dk, flux
+
+    def value(self, theta):
+        cfg = self.theta_cfg(theta)
+        hist = self.ctx.binned_forward(cfg, 0, self.n_batches, self.bins, self.seed, self.precision)
+        self.last_hist = hist
+        mu, k, _, flux = self._mu(hist, cfg)
+        lnl = -0.5 * float(np.sum((mu - self.data) ** 2 / self.var))
+        sigma = flux * float(hist[:, :5].sum(axis=0) @ k)
+        return lnl, sigma, mu
+
+    def gradient(self, theta):
+        lnl, sigma, mu = self.value(theta)
+        cfg = self.theta_cfg(theta)
+        r = -(mu - self.data) / self.var
+        g, s = self.ctx.binned_adjoint(cfg, 0, self.n_batches, self.bins, r, self.seed, self.precision)
+        _, dk, flux = coupling_factors(cfg)
+        return lnl, flux * g @ dk, sigma, flux * s @ dk
+
+    def analytic_gradient(self, theta, hist=None):
+        cfg = self.theta_cfg(theta)
+        hist = self.last_hist if hist is None else hist
+        mu, k, dk, flux = self._mu(hist, cfg)
+        r = -(mu - self.data) / self.var
+        R = hist[:, :5]
+        return flux * (r @ R) @ dk, flux * R.sum(axis=0) @ dk
 
 
 def run_simulation(cfg, rng="ranf", seed=None, jump_per_batch=False, sorting=True, precision=TP_PREC_FP64,

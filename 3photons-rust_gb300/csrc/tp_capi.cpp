@@ -78,6 +78,10 @@ struct tp_ctx {
   size_t dump_bytes = 0;
   unsigned int* d_err = nullptr;
   unsigned long long* d_recheck = nullptr;  // FP32-mixed events settled in FP64
+  double* d_hist = nullptr;   // binned forward: kMaxBins x kBinStride
+  double* d_binw = nullptr;   // adjoint: bin weights (kMaxBins)
+  double* d_adj = nullptr;    // adjoint: per-batch sums, kChunk x 10
+  int sms = 0;
   // optional CUDA-event timing of every kernel launch (tp_profile)
   int prof = 0;
   std::vector<cudaEvent_t> ev_pool;
@@ -164,9 +168,15 @@ int check_seed(tp_ctx* c, int rng_kind, uint64_t seed) {
   return TP_OK;
 }
 
+enum class Pass { kBatches, kBinned, kAdjoint };
+
 // Queues the batches on `stream`; `out` holds device pointers (stride n).
+// `pass` selects the per-batch accumulators, the binned forward pass or the
+// adjoint pass (the latter two take their extra fields from `extra`).
 int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
-              uint64_t n_batches, int precision, const BatchOut& out, cudaStream_t stream) {
+              uint64_t n_batches, int precision, const BatchOut& out, cudaStream_t stream,
+              Pass pass = Pass::kBatches, const KParams* extra = nullptr,
+              std::vector<double>* adj_host = nullptr) {
   if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
   if (int st = check_kind(c, rng_kind)) return st;
   if (int st = check_seed(c, rng_kind, seed)) return st;
@@ -190,6 +200,19 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
   kp.thread_poly = c->d_thread_poly;
+  if (extra) {
+    kp.nx = extra->nx;
+    kp.ny = extra->ny;
+    kp.x_lo = extra->x_lo;
+    kp.x_inv_w = extra->x_inv_w;
+    kp.y_lo = extra->y_lo;
+    kp.y_inv_w = extra->y_inv_w;
+    kp.bin_weight = c->d_binw;
+    kp.hist = c->d_hist;
+    kp.adj = c->d_adj;
+  }
+  if (pass != Pass::kBatches && kind != TP_RNG_XOSHIRO256P)
+    return c->fail(TP_ERR_UNSUPPORTED, "binned and adjoint passes use the xoshiro256+ stream");
   uint64_t start[4];
   xoshiro_seed(seed, start);
   for (uint64_t c0 = 0; c0 < n_batches; c0 += kChunk) {
@@ -223,13 +246,48 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     const int need = (kBatch + c->ept - 1) / c->ept;
     const int tpb = kind == TP_RNG_XOSHIRO256P ? ((need + 31) / 32) * 32 : kTpb;
     if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
-    st = launch_events(rng_kind, kp, tpb, stream);
+    if (pass == Pass::kBatches)
+      st = launch_events(rng_kind, kp, tpb, stream);
+    else if (pass == Pass::kBinned)
+      st = launch_binned(kp, tpb, 0, stream);
+    else
+      st = launch_adjoint(kp, tpb, stream);
     if (e1) {
       cudaEventRecord(e1, stream);
       c->prof_marks.push_back({1, {e0, e1}});
     }
     if (st) return c->fail(st, std::string("event launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (pass == Pass::kAdjoint && adj_host) {
+      const size_t off = adj_host->size();
+      adj_host->resize(off + 10 * cn);
+      st = c->cuda(cudaMemcpyAsync(adj_host->data() + off, c->d_adj, 10 * cn * sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream), "copy adjoint sums");
+      if (!st) st = c->cuda(cudaStreamSynchronize(stream), "adjoint");
+      if (st) return st;
+    }
   }
+  return TP_OK;
+}
+
+int binning_params(tp_ctx* c, const tp_config* cfg, const tp_binning* bins, KParams* kp) {
+  if (!bins || bins->n_emax < 1 || bins->n_cos < 1 || (int64_t)bins->n_emax * bins->n_cos > kMaxBins)
+    return c->fail(TP_ERR_INVALID, "binning: 1 <= n_emax * n_cos <= 1024");
+  double xl = bins->emax_lo, xh = bins->emax_hi, yl = bins->cos_lo, yh = bins->cos_hi;
+  if (xl == 0.0 && xh == 0.0) {
+    xl = cfg->e_total / 3.0;
+    xh = cfg->e_total / 2.0;
+  }
+  if (yl == 0.0 && yh == 0.0) {
+    yl = -cfg->beam_photons_cut;
+    yh = cfg->beam_photons_cut;
+  }
+  if (!(xh > xl) || !(yh > yl)) return c->fail(TP_ERR_INVALID, "binning: empty range");
+  kp->nx = bins->n_emax;
+  kp->ny = bins->n_cos;
+  kp->x_lo = xl;
+  kp->x_inv_w = bins->n_emax / (xh - xl);
+  kp->y_lo = yl;
+  kp->y_inv_w = bins->n_cos / (yh - yl);
   return TP_OK;
 }
 
@@ -265,6 +323,10 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
+  alloc((void**)&c->d_hist, kMaxBins * kBinStride * sizeof(double), "histogram");
+  alloc((void**)&c->d_binw, kMaxBins * sizeof(double), "bin weights");
+  alloc((void**)&c->d_adj, kChunk * 10 * sizeof(double), "adjoint sums");
+  if (!st) st = c->cuda(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "device query");
   alloc(&c->d_state, kChunk * 56 * 4, "batch states");
   (void)dummy;
   (void)p;
@@ -289,7 +351,8 @@ void tp_destroy(tp_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly,
-                  c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck};
+                  c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
+                  c->d_hist, c->d_binw, c->d_adj};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -341,12 +404,18 @@ int tp_run_batches(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed,
 
 int tp_dump_events(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_event, uint64_t n,
                    tp_event_dump* out) {
+  return tp_dump_events_prec(c, cfg, rng_kind, seed, first_event, n, TP_PREC_FP64, out);
+}
+
+int tp_dump_events_prec(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_event,
+                        uint64_t n, int precision, tp_event_dump* out) {
   if (!c) return TP_ERR_INVALID;
   if (!out) return c->fail(TP_ERR_INVALID, "null output array");
   if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
   if (int st = check_kind(c, rng_kind)) return st;
   if (int st = check_seed(c, rng_kind, seed)) return st;
   if (n == 0) return TP_OK;
+  if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED) return c->fail(TP_ERR_INVALID, "unknown precision");
   if (n > (1ull << 26) || first_event > (1ull << 50)) return c->fail(TP_ERR_INVALID, "dump range too large");
   cudaSetDevice(c->device);
   const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
@@ -359,7 +428,7 @@ int tp_dump_events(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed,
   xoshiro_seed(seed, start);
   int st = c->cuda(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "clear error word");
   if (st) return st;
-  st = launch_dump(rng_kind, k, start, c->d_ranf_window, (int32_t)seed, c->d_xo_draw, c->d_xo_jump, c->d_ranf_tab,
+  st = launch_dump(rng_kind, precision, k, start, c->d_ranf_window, (int32_t)seed, c->d_xo_draw, c->d_xo_jump, c->d_ranf_tab,
                    first_event, n, static_cast<tp_event_dump*>(c->d_dump), c->d_err, c->stream);
   if (st) return c->fail(st, std::string("dump launch: ") + cudaGetErrorString(cudaGetLastError()));
   unsigned int herr = 0;
@@ -374,6 +443,54 @@ int tp_set_events_per_thread(tp_ctx* c, int ept) {
   if (!c) return TP_ERR_INVALID;
   if (ept <= 0 || (TP_BATCH_SIZE + ept - 1) / ept > kTpb) return c->fail(TP_ERR_INVALID, "events per thread out of range");
   c->ept = ept;
+  return TP_OK;
+}
+
+int tp_binned_forward(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+                      uint64_t n_batches, int precision, const tp_binning* bins, double* out) {
+  if (!c) return TP_ERR_INVALID;
+  if (!out) return c->fail(TP_ERR_INVALID, "null output array");
+  if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
+  cudaSetDevice(c->device);
+  KParams kp{};
+  if (int st = binning_params(c, cfg, bins, &kp)) return st;
+  const size_t nbin = (size_t)kp.nx * kp.ny;
+  int st = c->cuda(cudaMemsetAsync(c->d_hist, 0, nbin * kBinStride * sizeof(double), c->stream), "clear histogram");
+  if (st) return st;
+  BatchOut none{};
+  st = run_async(c, cfg, rng_kind, seed, first_batch, n_batches, precision, none, c->stream, Pass::kBinned, &kp);
+  if (st) return st;
+  st = c->cuda(cudaMemcpyAsync(out, c->d_hist, nbin * kBinStride * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream), "copy histogram");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "binned forward");
+  return st;
+}
+
+int tp_binned_adjoint(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+                      uint64_t n_batches, int precision, const tp_binning* bins, const double* bin_weight,
+                      double g[5], double s_out[5]) {
+  if (!c) return TP_ERR_INVALID;
+  if (!bin_weight || !g || !s_out) return c->fail(TP_ERR_INVALID, "null array");
+  if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
+  cudaSetDevice(c->device);
+  KParams kp{};
+  if (int st = binning_params(c, cfg, bins, &kp)) return st;
+  const size_t nbin = (size_t)kp.nx * kp.ny;
+  int st = c->cuda(cudaMemcpyAsync(c->d_binw, bin_weight, nbin * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+                   "upload bin weights");
+  if (st) return st;
+  std::vector<double> per_batch;
+  per_batch.reserve(10 * (n_batches < kChunk ? n_batches : kChunk));
+  BatchOut none{};
+  st = run_async(c, cfg, rng_kind, seed, first_batch, n_batches, precision, none, c->stream, Pass::kAdjoint, &kp,
+                 &per_batch);
+  if (st) return st;
+  for (int k = 0; k < 5; ++k) g[k] = s_out[k] = 0.0;
+  for (uint64_t i = 0; i < n_batches; ++i)  // batch order
+    for (int k = 0; k < 5; ++k) {
+      g[k] += per_batch[10 * i + k];
+      s_out[k] += per_batch[10 * i + 5 + k];
+    }
   return TP_OK;
 }
 

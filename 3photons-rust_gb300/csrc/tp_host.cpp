@@ -267,6 +267,10 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   k.f_c2 = (float)k.c2;
   for (int c = 0; c < 4; ++c) k.f_sc_raw[c] = (float)k.sc_raw[c];
   for (int c = 0; c < 5; ++c) k.f_sc[c] = (float)k.sc[c];
+  for (int c = 0; c < 5; ++c) {
+    k.K[c] = k.sc_raw[c < 3 ? c : 3] * k.sc[c];
+    k.f_K[c] = (float)k.K[c];
+  }
   k.flags = flags;
   *out = k;
   return TP_OK;
@@ -569,3 +573,93 @@ int tp_format_report(const tp_config* cfg, const tp_final_results* r, char* buf,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// K_c(theta) and dK_c/dtheta for theta = (beta+, beta-, M_Z, Gamma_Z) by
+// forward-mode dual numbers through the same formulas as above
+// (src/coupling.rs:23-33, src/resacc.rs:59-100).
+// ---------------------------------------------------------------------------
+namespace tp {
+namespace {
+struct D4 {
+  double v;
+  double d[4];
+};
+D4 cst(double x) { return {x, {0, 0, 0, 0}}; }
+D4 var(double x, int i) {
+  D4 r = cst(x);
+  r.d[i] = 1.0;
+  return r;
+}
+D4 operator+(D4 a, D4 b) {
+  D4 r{a.v + b.v, {}};
+  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+D4 operator-(D4 a, D4 b) {
+  D4 r{a.v - b.v, {}};
+  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+D4 operator*(D4 a, D4 b) {
+  D4 r{a.v * b.v, {}};
+  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+D4 operator/(D4 a, D4 b) {
+  D4 r{a.v / b.v, {}};
+  for (int i = 0; i < 4; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) / (b.v * b.v);
+  return r;
+}
+D4 dsqrt(D4 a) {
+  D4 r{std::sqrt(a.v), {}};
+  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] / (2.0 * r.v);
+  return r;
+}
+}  // namespace
+}  // namespace tp
+
+extern "C" int tp_coupling_factors(const tp_config* cfg, double k_out[5], double dk_out[20], double* flux) {
+  using namespace tp;
+  if (check_config(cfg) || !k_out) return TP_ERR_INVALID;
+  const D4 bp = var(cfg->beta_plus, 0), bm = var(cfg->beta_minus, 1);
+  const D4 mz = var(cfg->m_z0, 2), gz = var(cfg->g_z0, 3);
+  // couplings and the spinor prefactor c1 (theta enters through M_Z only)
+  const double e2 = (4.0 * kPi) * cfg->alpha;
+  const double e2_z = (4.0 * kPi) * cfg->alpha_z;
+  const double cos2w = 1.0 - cfg->sin2_weinberg;
+  const D4 mz2 = mz * mz, mz4 = mz2 * mz2;
+  const D4 g_beta = cst(-std::sqrt(e2_z / ((4.0 * cos2w) * cfg->sin2_weinberg))) / mz4;
+  const double g_a = -powi(std::sqrt(e2), 3);
+  EvConst k;
+  make_ev_const(*cfg, 0, &k);
+  const D4 c1 = cst(k.c1);
+  const D4 ga_c1 = cst(g_a) * c1, gb_c1 = g_beta * c1;
+  const D4 sc_raw[4] = {ga_c1 * ga_c1, gb_c1 * gb_c1, gb_c1 * gb_c1, cst(-2.0) * cst(g_a) * g_beta * c1 * c1};
+  // sigma contributions
+  const double fact_com = (1.0 / 6.0) * cfg->gev2_to_picobarn;
+  const D4 rw = gz / mz;
+  const double p_ab = 1.0 - 4.0 * cfg->sin2_weinberg;
+  const double p_bb = p_ab + 8.0 * powi(cfg->sin2_weinberg, 2);
+  const D4 c_aa = cst(fact_com * 2.0);
+  const D4 c_ab = cst(fact_com * p_ab) / mz2;
+  const D4 c_bb = cst(fact_com * p_bb) / mz4;
+  const D4 ratio = cst(cfg->e_total) / mz;
+  const D4 dzeta = ratio * ratio;
+  const D4 delta = (dzeta - cst(1.0)) / rw;
+  const D4 prop = cst(1.0) / (cst(1.0) + delta * delta);
+  const double norm_weight = event_weight(cfg->e_total) * (std::pow(2.0 * kPi, -5.0) / (double)cfg->num_events);
+  const D4 com = cst(norm_weight / 4.0);
+  const D4 aa = com * c_aa;
+  const D4 bb = com * c_bb * prop / (rw * rw);
+  const D4 ab = com * c_ab * cst(2.0) * bp * prop / rw;
+  const D4 sc[5] = {aa, bb * bp * bp, bb * bm * bm, ab * delta, cst(0.0) - ab};
+  for (int c = 0; c < 5; ++c) {
+    const D4 K = sc_raw[c < 3 ? c : 3] * sc[c];
+    k_out[c] = K.v;
+    if (dk_out)
+      for (int i = 0; i < 4; ++i) dk_out[4 * c + i] = K.d[i];
+  }
+  if (flux) *flux = 1.0 / (2.0 * powi(cfg->e_total, 2));
+  return TP_OK;
+}

@@ -39,6 +39,9 @@ struct EvConst {
   float f_xx_in, f_fx_em, f_fx_ep, f_c1, f_c2;
   float f_sc_raw[4];
   float f_sc[5];
+  // per-event weight w = sum_c raw_c * K_c (K = sc_raw * sc, see above)
+  double K[5];
+  float f_K[5];
   int flags;  // TP_MODE_* bits
 };
 
@@ -64,7 +67,18 @@ struct KParams {
   BatchOut out;
   unsigned int* err;     // device error word (0 = fine)
   unsigned long long* recheck_count;  // FP32-mixed: events decided by the FP64 recheck
+  // binned observables: x = E of the most energetic photon, y = cosine of
+  // its angle to the electron beam; bin = ix * ny + iy
+  int nx, ny;
+  double x_lo, x_inv_w, y_lo, y_inv_w;
+  const double* bin_weight;  // adjoint: d lnL / d mu_b per bin
+  double* hist;              // binned forward: [nx * ny][8] accumulators
+  double* adj;               // adjoint: [n_batches][10] per-batch sums
 };
+
+// per-bin record of the binned forward pass
+constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
+constexpr int kMaxBins = 1024;
 
 // Host-side helpers (tp_host.cpp)
 int make_ev_const(const tp_config& cfg, int flags, EvConst* k);
@@ -78,12 +92,14 @@ int launch_seed_ranf(int jump_per_batch, int32_t seed, const int32_t* d_window,
                      const uint32_t* d_table, uint64_t first_batch, uint64_t n_batches,
                      int32_t* d_out, void* stream);
 int launch_events(int rng_kind, const KParams& p, int tpb, void* stream);
-int launch_dump(int rng_kind, const EvConst& k, const uint64_t start[4], const int32_t* d_window,
+int launch_dump(int rng_kind, int precision, const EvConst& k, const uint64_t start[4], const int32_t* d_window,
                 int32_t seed, const uint64_t* d_xo_draw_table, const uint64_t* d_xo_jump_table,
                 const uint32_t* d_ranf_table, uint64_t first_event, uint64_t n,
                 tp_event_dump* d_out, unsigned int* d_err, void* stream);
 
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
+int launch_binned(const KParams& p, int tpb, int grid, void* stream);
+int launch_adjoint(const KParams& p, int tpb, void* stream);
 
 }  // namespace tp
 

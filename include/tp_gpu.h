@@ -186,10 +186,57 @@ int tp_dump_events(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
                    uint64_t seed, uint64_t first_event, uint64_t n,
                    tp_event_dump *out);
 
+/* tp_dump_events for a given precision. With TP_PREC_FP32_MIXED the dump
+ * shows the FP32-mixed path's view of each event: FP32 momenta (widened),
+ * FP32 m2 sums, and `reserved` = 1 where the FP64 recheck decided the
+ * event's cuts. */
+int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                        uint64_t seed, uint64_t first_event, uint64_t n,
+                        int precision, tp_event_dump *out);
+
 /* Tuning: events each thread integrates in the xoshiro kernels (default
  * 40; ceil(10000 / ept) must not exceed 256). No counterpart in the
  * reference, whose batches run on one CPU thread each. */
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
+
+/* ---- binned observables and their adjoint ---------------------------------
+ * No counterpart in the reference (its histogram settings `num_bins`/`plot`
+ * are read but unused, src/config.rs:45-51, src/main.rs:122). Every kept
+ * event has the weight w = sum_c raw_c K_c(theta): raw_c, the five unscaled
+ * helicity sums of the event (A, B+, B-, Re and Im of the mixed term,
+ * src/matelems.rs:53-86), depend only on its kinematics; K_c, the couplings
+ * times the sigma contributions (src/coupling.rs:23-33,
+ * src/resacc.rs:59-100), on theta = (beta+, beta-, M_Z, Gamma_Z). Bins:
+ * x = energy of the most energetic photon, y = cosine of its angle to the
+ * electron beam; bin index ix * n_cos + iy; values outside the range go to
+ * the edge bins. Both passes use the xoshiro256+ stream. */
+typedef struct tp_binning {
+  int32_t n_emax, n_cos;    /* n_emax * n_cos <= 1024                       */
+  double emax_lo, emax_hi;  /* GeV; both 0: [sqrt(s)/3, sqrt(s)/2]           */
+  double cos_lo, cos_hi;    /* both 0: [-ACUT, ACUT]                         */
+} tp_binning;
+
+/* Forward pass: per bin, 8 sums [raw_0..raw_4, events, w, w^2] (w at the
+ * theta of cfg) into the caller's host array of n_emax * n_cos * 8. */
+int tp_binned_forward(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                      uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+                      int precision, const tp_binning *bins, double *out);
+
+/* Adjoint pass: recomputes every event from its stream position and returns
+ * g_c = sum_e r[bin(e)] raw_c,e and s_c = sum_e raw_c,e, where r is the
+ * caller's per-bin weight (for a likelihood L: r_b = d lnL / d mu_b). With
+ * flux and dK from tp_coupling_factors: d lnL/dtheta = flux sum_c g_c dK_c,
+ * d sigma/dtheta = flux sum_c s_c dK_c. Batches are summed in order. */
+int tp_binned_adjoint(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                      uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+                      int precision, const tp_binning *bins,
+                      const double *bin_weight, double g[5], double s[5]);
+
+/* K_c(theta) and dK_c/d(beta+, beta-, M_Z, Gamma_Z) (dk[4 c + i], forward-
+ * mode dual numbers) at the theta of cfg, and the incident flux 1/(2 s)
+ * (src/resacc.rs:178) that turns sums of w into cross sections (pb). */
+int tp_coupling_factors(const tp_config *cfg, double k[5], double dk[20],
+                        double *flux);
 
 /* ---- measurement (no counterpart in the reference, which only measures
  * its wall-clock time, src/main.rs:85,138) ------------------------------

@@ -802,19 +802,23 @@ int tpo_dump_events(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
   const int flags = rng_kind & ~TP_RNG_KIND_MASK;
   if (flags & TPO_MODE_FASTER_EVGEN) return TP_ERR_UNSUPPORTED;
   const Consts k = make_consts(*cfg);
-  Rng rng;
+  Rng rng, sched;  // sched: the scheduler's copy, jumped once per batch
   rng.init(rng_kind & TP_RNG_KIND_MASK, seed);
   uint64_t e = 0;
   if (flags & TP_MODE_JUMP_PER_BATCH) {
     const uint64_t b = first_event / kBatch;
     for (uint64_t j = 0; j < b; ++j) rng.jump();
+    sched = rng;
     e = b * kBatch;
   }
   for (; e < first_event; ++e)
     for (int i = 0; i < 12; ++i) rng.random();
   Event ev;
   for (uint64_t i = 0; i < n; ++i, ++e) {
-    if ((flags & TP_MODE_JUMP_PER_BATCH) && e % kBatch == 0 && i > 0) rng.jump();
+    if ((flags & TP_MODE_JUMP_PER_BATCH) && e % kBatch == 0 && i > 0) {
+      sched.jump();
+      rng = sched;
+    }
     tp_event_dump& d = out[i];
     std::memset(&d, 0, sizeof d);
     generate(k, rng, flags, ev, d.uniforms);
@@ -824,6 +828,21 @@ int tpo_dump_events(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
     if (d.cut == 0) m2_sums(k, ev, d.m2_sums);
   }
   return TP_OK;
+}
+
+// MEsContributions::m2_sums of given photon momenta ([photon][X,Y,Z,E])
+void tpo_m2_sums_of(const tp_config* cfg, const double* p_out, double out[5]) {
+  const Consts k = make_consts(*cfg);
+  Event ev;
+  const double h = cfg->e_total / 2.0;
+  const double beams[2][4] = {{-cfg->e_total / 2.0, 0.0, 0.0, h}, {h, 0.0, 0.0, h}};
+  for (int c = 0; c < 4; ++c) {
+    ev.p[0][c] = beams[0][c];
+    ev.p[1][c] = beams[1][c];
+  }
+  for (int p = 0; p < 3; ++p)
+    for (int c = 0; c < 4; ++c) ev.p[2 + p][c] = p_out[4 * p + c];
+  m2_sums(k, ev, out);
 }
 
 // Per-batch accumulators of batches [first_batch, first_batch + n_batches),
@@ -892,6 +911,61 @@ int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
       }
     });
   for (auto& th : pool) th.join();
+  return TP_OK;
+}
+
+// Per-bin sums of the kept events of batches [first_batch, first_batch + n):
+// out[bin][0..4] = m2_sums, [5] = events, [6] = sum w, [7] = sum w^2, with
+// w = m2_sums . sigma_contribs (resacc.rs:126). Bin: ix * ny + iy with x =
+// E of the most energetic photon, y = -p_x / E of it (cosine to the e-).
+int tpo_binned(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches, int nx,
+               int ny, double xlo, double xhi, double ylo, double yhi, double* out) {
+  if (!cfg_ok(cfg) || !out || nx < 1 || ny < 1) return TP_ERR_INVALID;
+  const int flags = rng_kind & ~TP_RNG_KIND_MASK;
+  const Consts k = make_consts(*cfg);
+  const double xinv = nx / (xhi - xlo), yinv = ny / (yhi - ylo);
+  for (int i = 0; i < nx * ny * 8; ++i) out[i] = 0.0;
+  Rng rng, sched;
+  rng.init(rng_kind & TP_RNG_KIND_MASK, seed);
+  sched = rng;
+  for (uint64_t b = 0; b < first_batch; ++b) {
+    if (flags & TP_MODE_JUMP_PER_BATCH) {
+      sched.jump();
+      rng = sched;
+    } else {
+      skip_batch(rng, flags, batch_size(*cfg, b));
+    }
+  }
+  Event ev;
+  for (uint64_t i = 0; i < n_batches; ++i) {
+    const uint64_t n = batch_size(*cfg, first_batch + i);
+    for (uint64_t e = 0; e < n; ++e) {
+      generate(k, rng, flags, ev, nullptr);
+      if (cut(*cfg, flags, ev) != 0) continue;
+      double m[5];
+      m2_sums(k, ev, m);
+      int l = 0;
+      if (ev.p[3][3] > ev.p[2 + l][3]) l = 1;
+      if (ev.p[4][3] > ev.p[2 + l][3]) l = 2;
+      const double en = ev.p[2 + l][3], c = -ev.p[2 + l][0] / en;
+      int ix = (int)std::floor((en - xlo) * xinv), iy = (int)std::floor((c - ylo) * yinv);
+      ix = ix < 0 ? 0 : (ix >= nx ? nx - 1 : ix);
+      iy = iy < 0 ? 0 : (iy >= ny ? ny - 1 : iy);
+      double* o = out + 8 * (ix * ny + iy);
+      double w = 0.0;
+      for (int cc = 0; cc < 5; ++cc) {
+        o[cc] += m[cc];
+        w += m[cc] * k.sigma_contribs[cc];
+      }
+      o[5] += 1.0;
+      o[6] += w;
+      o[7] += w * w;
+    }
+    if (flags & TP_MODE_JUMP_PER_BATCH) {
+      sched.jump();
+      rng = sched;
+    }
+  }
   return TP_OK;
 }
 

@@ -22,8 +22,11 @@ void tpo_xoshiro_jump128(uint64_t state[4]);
 void tpo_ranf_state(int32_t seed, uint64_t resets, int32_t out[56]);
 int tpo_dump_events(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_event, uint64_t n,
                     tp_event_dump* out);
+void tpo_m2_sums_of(const tp_config* cfg, const double* p_out, double out[5]);
 int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
                     tp_batch_soa* out, int threads);
+int tpo_binned(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches, int nx,
+               int ny, double xlo, double xhi, double ylo, double yhi, double* out);
 int tpo_merge_finalize(const tp_config* cfg, const tp_batch_soa* b, uint64_t n, tp_final_results* res);
 int tpo_format_res_data(const tp_config* cfg, const tp_final_results* r, char* buf, size_t len);
 int tpo_format_report(const tp_config* cfg, const tp_final_results* r, char* buf, size_t len);

@@ -42,7 +42,10 @@ def lib(pkg):
         L.tpo_xoshiro_jump128.argtypes = [P(ctypes.c_uint64)]
         L.tpo_ranf_state.argtypes = [ctypes.c_int32, u64, P(ctypes.c_int32)]
         L.tpo_dump_events.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, vp]
+        L.tpo_m2_sums_of.argtypes = [P(pkg.CConfig), P(ctypes.c_double), P(ctypes.c_double)]
         L.tpo_run_batches.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, P(pkg.CBatchSoa), i32]
+        d = ctypes.c_double
+        L.tpo_binned.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, i32, i32, d, d, d, d, vp]
         L.tpo_merge_finalize.argtypes = [P(pkg.CConfig), P(pkg.CBatchSoa), u64, P(pkg.CFinalResults)]
         L.tpo_format_res_data.argtypes = [P(pkg.CConfig), P(pkg.CFinalResults), ctypes.c_char_p, ctypes.c_size_t]
         L.tpo_format_report.argtypes = [P(pkg.CConfig), P(pkg.CFinalResults), ctypes.c_char_p, ctypes.c_size_t]
@@ -74,6 +77,22 @@ class Oracle:
         out = np.zeros(n, self.pkg.DUMP_DTYPE)
         st = self.L.tpo_dump_events(ctypes.byref(cfg.c), rng_kind, seed, first_event, n,
                                     ctypes.c_void_p(out.ctypes.data))
+        assert st == 0, st
+        return out
+
+    def m2_sums_of(self, cfg, p_out):
+        """m2_sums of the photons p_out[n, 3, 4] (one row per event)."""
+        p = np.ascontiguousarray(p_out, np.float64)
+        out = np.zeros((p.shape[0], 5), np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        for i in range(p.shape[0]):
+            self.L.tpo_m2_sums_of(ctypes.byref(cfg.c), p[i].ctypes.data_as(dp), out[i].ctypes.data_as(dp))
+        return out
+
+    def binned(self, cfg, rng_kind, seed, first_batch, n_batches, nx, ny, xr, yr):
+        out = np.zeros((nx * ny, 8), np.float64)
+        st = self.L.tpo_binned(ctypes.byref(cfg.c), rng_kind, seed, first_batch, n_batches, nx, ny, xr[0], xr[1],
+                               yr[0], yr[1], ctypes.c_void_p(out.ctypes.data))
         assert st == 0, st
         return out
 

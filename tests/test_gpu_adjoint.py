@@ -1,0 +1,106 @@
+"""The differentiation form: binned forward pass against the CPU
+restatement; the adjoint pass against the analytic gradient of the
+accumulated per-bin coefficient sums and against central finite
+differences (h = 1e-4); the torch.autograd.Function wrapper; a gradient fit
+that recovers beta+ and |beta-|."""
+import numpy as np
+import pytest
+import torch
+
+from tp_autograd import log_likelihood
+
+pytestmark = pytest.mark.gpu
+
+SEED_DATA, SEED_MODEL = 777, 12345
+
+
+@pytest.fixture(scope="module")
+def setup(tp, ctx, cfg_sqrts1000):
+    bins = tp.binning(20, 20)
+    data_cfg = cfg_sqrts1000.replace(num_events=4_000_000, beta_plus=0.3, beta_minus=-0.2)
+    data = ctx.binned_forward(data_cfg, 0, data_cfg.num_batches, bins, SEED_DATA)
+    model_cfg = cfg_sqrts1000.replace(num_events=1_000_000, beta_plus=0.0, beta_minus=0.0)
+    model = tp.BinnedGaussianLikelihood(ctx, model_cfg, SEED_MODEL, model_cfg.num_batches, data, data_cfg, bins)
+    return bins, data_cfg, data, model_cfg, model
+
+
+def test_binned_forward_matches_restatement(tp, oracle, ctx, cfg_sqrts1000):
+    cfg = cfg_sqrts1000.replace(num_events=200_000)
+    bins = tp.binning(20, 20)
+    gpu = ctx.binned_forward(cfg, 0, cfg.num_batches, bins, SEED_MODEL)
+    e = cfg.e_total
+    ref = oracle.binned(cfg, tp.rng_flags("xoshiro"), SEED_MODEL, 0, cfg.num_batches, 20, 20, (e / 3, e / 2),
+                        (-cfg.beam_photons_cut, cfg.beam_photons_cut))
+    assert np.array_equal(gpu[:, 5], ref[:, 5])  # events per bin
+    k, _, _ = tp.coupling_factors(cfg)
+    sc = np.array(oracle.sigma_contribs(cfg))
+    sc_raw = k / sc  # per-contribution coupling factor (all sc != 0 off the Z peak)
+    m_gpu = gpu[:, :5] * sc_raw
+    tot = np.abs(ref[:, :5]).sum(axis=0)
+    assert np.all(np.abs(m_gpu - ref[:, :5]).sum(axis=0) <= 1e-11 * tot)
+    assert np.allclose(gpu[:, 6], ref[:, 6], rtol=1e-11, atol=1e-11 * np.abs(ref[:, 6]).max())
+    assert np.allclose(gpu[:, 7], ref[:, 7], rtol=1e-11, atol=1e-11 * np.abs(ref[:, 7]).max())
+    # and the binned total is the cross-section sum of the batch path
+    acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", seed=SEED_MODEL)
+    assert abs(gpu[:, 6].sum() - acc.sigma.sum()) <= 1e-12 * abs(acc.sigma.sum())
+
+
+@pytest.mark.parametrize("theta", [(0.0, 0.0, 91.187, 2.49), (0.25, -0.1, 91.187, 2.49), (1.0, 1.0, 91.0, 2.6)])
+def test_adjoint_matches_analytic_gradient(setup, theta):
+    _, _, _, _, model = setup
+    lnl, grad, sigma, dsigma = model.gradient(theta)
+    ga, dsa = model.analytic_gradient(theta)
+    assert np.allclose(grad, ga, rtol=1e-10, atol=1e-10 * np.abs(ga).max())
+    assert np.allclose(dsigma, dsa, rtol=1e-10, atol=1e-10 * np.abs(dsa).max())
+
+
+def test_adjoint_matches_central_differences(setup):
+    _, _, _, _, model = setup
+    theta = np.array([0.25, -0.1, 91.187, 2.49])
+    _, grad, _, dsigma = model.gradient(theta)
+    for i in range(4):
+        h = 1e-4 * max(abs(theta[i]), 1.0)
+        tp_, tm = theta.copy(), theta.copy()
+        tp_[i] += h
+        tm[i] -= h
+        lp, sp, _ = model.value(tp_)
+        lm, sm, _ = model.value(tm)
+        fd, fds = (lp - lm) / (2 * h), (sp - sm) / (2 * h)
+        assert abs(fd - grad[i]) <= 1e-5 * max(abs(grad[i]), 1e-3 * np.abs(grad).max()), (i, fd, grad[i])
+        assert abs(fds - dsigma[i]) <= 1e-5 * max(abs(dsigma[i]), 1e-3 * np.abs(dsigma).max()), (i, fds, dsigma[i])
+
+
+def test_fp32_adjoint_close_to_fp64(tp, setup):
+    bins, data_cfg, data, model_cfg, model = setup
+    m32 = tp.BinnedGaussianLikelihood(model.ctx, model_cfg, SEED_MODEL, model.n_batches, data, data_cfg, bins,
+                                      precision=tp.TP_PREC_FP32_MIXED)
+    theta = (0.25, -0.1, 91.187, 2.49)
+    l64, g64, s64, ds64 = model.gradient(theta)
+    l32, g32, s32, ds32 = m32.gradient(theta)
+    assert abs(s32 - s64) <= 1e-6 * abs(s64)
+    assert np.all(np.abs(g32 - g64) <= 1e-5 * np.abs(g64).max())
+
+
+def test_torch_autograd_function(setup):
+    _, _, _, _, model = setup
+    theta = torch.tensor([0.25, -0.1, 91.187, 2.49], dtype=torch.float64, requires_grad=True)
+    lnl = log_likelihood(theta, model)
+    lnl.backward()
+    _, grad, _, _ = model.gradient(theta.detach().tolist())
+    assert torch.allclose(theta.grad, torch.tensor(grad), rtol=1e-12)
+
+
+def test_gradient_fit_recovers_betas(setup):
+    # 200 gradient-ascent steps on (beta+, beta-) from a small offset of the
+    # model point beta+- = 0 (beta- = 0 is a stationary point: only beta-^2
+    # enters the weights, so |beta-| is what the data determine)
+    _, _, _, _, model = setup
+    theta = np.array([0.0, 0.05, 91.187, 2.49])
+    _, g0, _, _ = model.gradient(theta)
+    lr = 0.02 / max(np.abs(g0[:2]).max(), 1e-300)
+    m = np.zeros(2)
+    for _ in range(200):
+        _, g, _, _ = model.gradient(theta)
+        m = 0.8 * m + g[:2]
+        theta[:2] += lr * m / (1 + 0.0 * np.abs(m))
+    assert abs(theta[0] - 0.3) < 0.03 and abs(abs(theta[1]) - 0.2) < 0.03, theta

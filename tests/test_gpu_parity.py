@@ -94,8 +94,18 @@ def test_event_dumps(tp, oracle, ctx, cfg_valeurs, rng, jump, sort):
     assert np.mean(d <= 8 * ulp) > 0.99
     kept = r["cut"] == 0
     m_g, m_r = g["m2_sums"][kept], r["m2_sums"][kept]
+    # amplitude algebra: the GPU's m2 against the restatement's formulas
+    # evaluated on the GPU's own momenta
+    m_same = oracle.m2_sums_of(cfg_valeurs, g["p_out"][kept][:2000])
+    scale = np.maximum(np.abs(m_same), np.abs(m_same[:, :1]))
+    alg = np.abs(m_g[:2000] - m_same) / scale
+    # photons close to the -z axis (xx = sqrt(E + Z) cancels) amplify the
+    # rounding differences of two equivalent formulas
+    assert np.max(alg) < 1e-10 and np.quantile(alg, 0.99) < 1e-13
+    # end to end: bounded by the conditioning of the momenta (above)
     scale = np.maximum(np.abs(m_r), np.abs(m_r[:, :1]))
-    assert np.max(np.abs(m_g - m_r) / scale) < 1e-12
+    err = np.abs(m_g - m_r) / scale
+    assert np.max(err) < 1e-9 and np.median(err) < 1e-14
 
 
 @pytest.mark.parametrize("features,rng,jump,sort", [
