@@ -166,6 +166,9 @@ def library():
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
         "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
+        "tp_run_points": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_uint64), i32, i32,
+                                P(ctypes.c_uint64), P(CBatchSoa), u64]),
+        "tp_autotune": (i32, [vp, P(CConfig), i32, u64, P(ctypes.c_int), P(ctypes.c_double)]),
         "tp_binned_forward": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp]),
         "tp_binned_adjoint": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp,
                                     P(ctypes.c_double), P(ctypes.c_double)]),
@@ -421,6 +424,40 @@ class Context:
                                                   seed, first_batch, n_batches, precision, ctypes.byref(soa),
                                                   ctypes.c_void_p(stream)))
 
+    def autotune(self, cfg, precision=TP_PREC_FP32_MIXED, sample_batches=2048):
+        """Picks events per thread (hence the block shape) for this context."""
+        ept, rate = ctypes.c_int(), ctypes.c_double()
+        self.check(library().tp_autotune(self.h, ctypes.byref(cfg.c), precision, sample_batches, ctypes.byref(ept),
+                                         ctypes.byref(rate)))
+        return ept.value, rate.value
+
+    def run_points(self, cfgs, starts, precision=TP_PREC_FP32_MIXED, sorting=True):
+        """Batched form: every point's run in one persistent launch (CUDA
+        graph). starts: [n_points, 4] raw xoshiro states. Returns one
+        BatchAccumulators per point."""
+        n = len(cfgs)
+        arr = (CConfig * n)(*[c.c for c in cfgs])
+        st = np.ascontiguousarray(starts, np.uint64).reshape(n, 4)
+        total = sum((c.num_events + TP_BATCH_SIZE - 1) // TP_BATCH_SIZE for c in cfgs)
+        acc = BatchAccumulators(total)
+        unit0 = np.zeros(n + 1, np.uint64)
+        soa = acc.soa()
+        self.check(library().tp_run_points(self.h, n, arr, st.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                           0 if sorting else TP_MODE_NO_PHOTON_SORTING, precision,
+                                           unit0.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.byref(soa),
+                                           total))
+        out = []
+        for p in range(n):
+            a, b = int(unit0[p]), int(unit0[p + 1])
+            part = BatchAccumulators(b - a)
+            part.selected[:] = acc.selected[a:b]
+            part.spm2[:] = acc.spm2[:, a:b]
+            part.vars[:] = acc.vars[:, a:b]
+            part.sigma[:] = acc.sigma[a:b]
+            part.variance[:] = acc.variance[a:b]
+            out.append(part)
+        return out
+
     def binned_forward(self, cfg, first_batch, n_batches, binning, seed=XOSHIRO_DEFAULT_SEED,
                        precision=TP_PREC_FP64, jump_per_batch=False):
         """Per-bin sums [n_bins, 8]: raw R_0..R_4, events, sum w, sum w^2."""
@@ -524,6 +561,59 @@ class BinnedGaussianLikelihood:
         r = -(mu - self.data) / self.var
         R = hist[:, :5]
         return flux * (r @ R) @ dk, flux * R.sum(axis=0) @ dk
+
+
+def xoshiro_start(seed, jumps128=0, draws=0):
+    """Raw xoshiro256+ state: seed_from_u64(seed), then jumps of 2^128."""
+    s = (ctypes.c_uint64 * 4)()
+    _check(library().tp_xoshiro_state_at(seed, jumps128, draws, s))
+    return list(s)
+
+
+def scan_points(base, n_points=256, seed=12345):
+    """Parameter points of the batched form: sqrt(s) ~ U[200, 2000] GeV,
+    E_min ~ U[1, 50] GeV, the |cos| cuts (beam-photon and photon-photon) ~
+    U[0.80, 0.99], beta+, beta- ~ U[-1, 1], events ~ log-U[1e6, 1e8], drawn
+    with numpy's PCG64(seed); everything else from `base`. Point p's stream
+    is xoshiro256+ seeded with 12345 and jumped p times by 2^128."""
+    r = np.random.Generator(np.random.PCG64(seed))
+    cfgs, starts = [], []
+    for p in range(n_points):
+        cut = float(r.uniform(0.80, 0.99))
+        cfgs.append(base.replace(e_total=float(r.uniform(200.0, 2000.0)), e_min=float(r.uniform(1.0, 50.0)),
+                                 beam_photons_cut=cut, photon_photon_cut=cut,
+                                 beta_plus=float(r.uniform(-1.0, 1.0)), beta_minus=float(r.uniform(-1.0, 1.0)),
+                                 num_events=int(np.exp(r.uniform(np.log(1e6), np.log(1e8))))))
+        starts.append(xoshiro_start(XOSHIRO_DEFAULT_SEED, p))
+    return cfgs, np.array(starts, np.uint64)
+
+
+def fisher_matrix(model, theta, hist=None):
+    """Gauss-Newton Fisher matrix J^T V^-1 J of a BinnedGaussianLikelihood,
+    J_bj = d mu_b / d theta_j = flux sum_c R_bc dK_c/dtheta_j, from the
+    forward pass's per-bin raw sums."""
+    cfg = model.theta_cfg(theta)
+    hist = model.last_hist if hist is None else hist
+    _, dk, flux = coupling_factors(cfg)
+    J = flux * hist[:, :5] @ dk
+    return J.T @ (J / model.var[:, None])
+
+
+def fit(model, theta0, steps=200, lr=0.5, free=(0, 1), damping=1e-3):
+    """Maximises ln L over the parameters `free` (indices into theta) with
+    `steps` natural-gradient steps: theta += lr (F + damping) ^-1 g, where g
+    comes from the forward + adjoint passes on the GPU and F is the
+    Gauss-Newton Fisher matrix of the same forward pass. Returns (theta,
+    covariance estimate F^-1 at the end)."""
+    theta = np.array(theta0, np.float64)
+    idx = list(free)
+    F = None
+    for _ in range(steps):
+        _, g, _, _ = model.gradient(theta)
+        F = fisher_matrix(model, theta)[np.ix_(idx, idx)]
+        Fd = F + damping * np.trace(F) / len(idx) * np.eye(len(idx))
+        theta[idx] += lr * np.linalg.solve(Fd, g[idx])
+    return theta, np.linalg.inv(F)
 
 
 def run_simulation(cfg, rng="ranf", seed=None, jump_per_batch=False, sorting=True, precision=TP_PREC_FP64,

@@ -56,7 +56,8 @@ def build(verbose=False, extra_nvcc=()):
         for o in outs:
             if o.strip():
                 print(o)
-    objs = [os.path.join(BUILD, s + ".o") for s in ("tp_kernels.cu", "tp_capi.cpp", "tp_host.cpp", "tp_rng.cpp")]
+    objs = [os.path.join(BUILD, s + ".o")
+            for s in ("tp_kernels.cu", "tp_capi.cpp", "tp_host.cpp", "tp_rng.cpp")]
     cudalib = ["-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart"]
     _run([nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, *cudalib])
     os.replace(LIB + ".tmp", LIB)

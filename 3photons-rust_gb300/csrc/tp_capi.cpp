@@ -17,6 +17,7 @@ using namespace tp;
 
 thread_local std::string g_create_error;
 
+
 // Batches per launch: bounds the device scratch (batch start states) to
 // 64 Ki batches = 14.7 MB (ranf) or 2 MB (xoshiro).
 constexpr uint64_t kChunk = 1ull << 16;
@@ -82,6 +83,14 @@ struct tp_ctx {
   double* d_binw = nullptr;   // adjoint: bin weights (kMaxBins)
   double* d_adj = nullptr;    // adjoint: per-batch sums, kChunk x 10
   int sms = 0;
+  // batched form (tp_run_points): device buffers and the captured graph
+  struct Points {
+    void* buf = nullptr;  // points, events, unit0, starts, unit_point, states, outputs, counter
+    size_t bytes = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key[6] = {0, 0, 0, 0, 0, 0};  // n_points, n_units, precision, ept, flags, buffer
+  } pts;
   // optional CUDA-event timing of every kernel launch (tp_profile)
   int prof = 0;
   std::vector<cudaEvent_t> ev_pool;
@@ -356,6 +365,9 @@ void tp_destroy(tp_ctx* c) {
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  if (c->pts.exec) cudaGraphExecDestroy(c->pts.exec);
+  if (c->pts.graph) cudaGraphDestroy(c->pts.graph);
+  if (c->pts.buf) cudaFree(c->pts.buf);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -491,6 +503,170 @@ int tp_binned_adjoint(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t se
       g[k] += per_batch[10 * i + k];
       s_out[k] += per_batch[10 * i + 5 + k];
     }
+  return TP_OK;
+}
+
+int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uint64_t* starts, int mode_flags,
+                  int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
+  if (!c) return TP_ERR_INVALID;
+  if (!cfgs || !starts || !unit0 || !out || !out->selected || !out->spm2 || !out->vars || !out->sigma ||
+      !out->variance)
+    return c->fail(TP_ERR_INVALID, "null array");
+  if (n_points == 0 || n_points > (1u << 20)) return c->fail(TP_ERR_INVALID, "n_points out of range");
+  if (mode_flags & ~TP_MODE_NO_PHOTON_SORTING) return c->fail(TP_ERR_INVALID, "unsupported mode flag");
+  if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED) return c->fail(TP_ERR_INVALID, "unknown precision");
+  cudaSetDevice(c->device);
+  // units: every point's batches, point by point
+  std::vector<EvConst> pk(n_points);
+  std::vector<uint64_t> pev(n_points);
+  uint64_t n_units = 0;
+  for (uint32_t p = 0; p < n_points; ++p) {
+    if (check_config(&cfgs[p])) return c->fail(TP_ERR_INVALID, "invalid configuration of point " + std::to_string(p));
+    make_ev_const(cfgs[p], mode_flags, &pk[p]);
+    pev[p] = cfgs[p].num_events;
+    unit0[p] = n_units;
+    n_units += (cfgs[p].num_events + kBatch - 1) / kBatch;
+  }
+  unit0[n_points] = n_units;
+  if (n_units > capacity) return c->fail(TP_ERR_INVALID, "output capacity below the number of batches");
+  if (n_units > (1ull << 31)) return c->fail(TP_ERR_INVALID, "too many batches");
+  std::vector<uint32_t> unit_point(n_units);
+  for (uint32_t p = 0; p < n_points; ++p)
+    for (uint64_t u = unit0[p]; u < unit0[p + 1]; ++u) unit_point[u] = p;
+  if (int st = ensure_thread_poly(c, c->ept)) return st;
+  // one device buffer, 256-byte aligned sections
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_pts = 0, o_ev = o_pts + al(n_points * sizeof(EvConst)), o_u0 = o_ev + al(n_points * 8),
+               o_st = o_u0 + al(n_points * 8), o_up = o_st + al(n_points * 32), o_us = o_up + al(n_units * 4),
+               o_out = o_us + al(n_units * 32), o_cnt = o_out + al(n_units * 13 * 8), total = o_cnt + 256;
+  if (c->pts.bytes < total) {
+    if (c->pts.buf) cudaFree(c->pts.buf);
+    c->pts.buf = nullptr;
+    c->pts.bytes = 0;
+    if (int st = c->cuda(cudaMalloc(&c->pts.buf, total), "points buffers")) return st;
+    c->pts.bytes = total;
+  }
+  char* base = static_cast<char*>(c->pts.buf);
+  PointsParams pp{};
+  pp.points = reinterpret_cast<const EvConst*>(base + o_pts);
+  pp.point_events = reinterpret_cast<const uint64_t*>(base + o_ev);
+  pp.point_unit0 = reinterpret_cast<const uint64_t*>(base + o_u0);
+  pp.point_start = reinterpret_cast<const uint64_t*>(base + o_st);
+  pp.unit_point = reinterpret_cast<const uint32_t*>(base + o_up);
+  pp.unit_state = reinterpret_cast<uint64_t*>(base + o_us);
+  pp.batch_table = c->d_xo_batch;
+  pp.thread_poly = c->d_thread_poly;
+  pp.counter = reinterpret_cast<unsigned long long*>(base + o_cnt);
+  pp.recheck_count = c->d_recheck;
+  auto* sel = reinterpret_cast<uint64_t*>(base + o_out);
+  auto* f = reinterpret_cast<double*>(sel + n_units);
+  pp.out = BatchOut{sel, f, f + 5 * n_units, f + 10 * n_units, f + 11 * n_units, n_units};
+  pp.n_units = n_units;
+  pp.ept = c->ept;
+  pp.precision = precision;
+  int st = TP_OK;
+  auto up = [&](size_t off, const void* src, size_t n) {
+    if (!st) st = c->cuda(cudaMemcpyAsync(base + off, src, n, cudaMemcpyHostToDevice, c->stream), "upload points");
+  };
+  up(o_pts, pk.data(), n_points * sizeof(EvConst));
+  up(o_ev, pev.data(), n_points * 8);
+  up(o_u0, unit0, n_points * 8);
+  up(o_st, starts, n_points * 32);
+  up(o_up, unit_point.data(), n_units * 4);
+  if (st) return st;
+  // the seeding + persistent launches are captured once per shape and replayed
+  const uint64_t key[6] = {n_points, n_units, (uint64_t)precision, (uint64_t)c->ept, (uint64_t)mode_flags,
+                           (uint64_t)(uintptr_t)c->pts.buf};
+  if (!c->pts.exec || std::memcmp(key, c->pts.key, sizeof key) != 0) {
+    if (c->pts.exec) cudaGraphExecDestroy(c->pts.exec);
+    if (c->pts.graph) cudaGraphDestroy(c->pts.graph);
+    c->pts.exec = nullptr;
+    c->pts.graph = nullptr;
+    const int need = (kBatch + c->ept - 1) / c->ept;
+    const int tpb = ((need + 31) / 32) * 32;
+    st = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    if (st) return st;
+    cudaMemsetAsync(pp.counter, 0, sizeof(unsigned long long), c->stream);
+    const int lst = launch_points(pp, tpb, c->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (lst || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return c->fail(TP_ERR_CUDA, "capturing the points launch failed");
+    }
+    st = c->cuda(cudaGraphInstantiate(&c->pts.exec, g, 0), "graph instantiate");
+    if (st) {
+      cudaGraphDestroy(g);
+      return st;
+    }
+    c->pts.graph = g;
+    std::memcpy(c->pts.key, key, sizeof key);
+  }
+  if (c->prof) {
+    cudaEvent_t e0 = c->next_event(), e1 = c->next_event();
+    if (e0 && e1) {
+      cudaEventRecord(e0, c->stream);
+      st = c->cuda(cudaGraphLaunch(c->pts.exec, c->stream), "graph launch");
+      cudaEventRecord(e1, c->stream);
+      c->prof_marks.push_back({1, {e0, e1}});
+    }
+  } else {
+    st = c->cuda(cudaGraphLaunch(c->pts.exec, c->stream), "graph launch");
+  }
+  if (st) return st;
+  const size_t n = n_units;
+  st = c->cuda(cudaMemcpyAsync(out->selected, sel, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->spm2, pp.out.spm2, 5 * n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->vars, pp.out.vars, 5 * n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->sigma, pp.out.sigma, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaMemcpyAsync(out->variance, pp.out.variance, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "run points");
+  return st;
+}
+
+int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_batches, int* best_ept,
+                double* best_events_per_s) {
+  if (!c) return TP_ERR_INVALID;
+  if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
+  if (sample_batches == 0 || sample_batches > kChunk) return c->fail(TP_ERR_INVALID, "sample_batches out of range");
+  cudaSetDevice(c->device);
+  // events per thread -> threads per CTA = ceil(10000 / ept) rounded to warps
+  static const int candidates[] = {40, 42, 48, 56, 64, 80, 100, 125};
+  const size_t n = sample_batches;
+  if (int st = ensure(c, &c->d_out, &c->out_bytes, n * 13 * 8, "output buffers")) return st;
+  auto* sel = static_cast<uint64_t*>(c->d_out);
+  auto* f = reinterpret_cast<double*>(sel + n);
+  BatchOut o{sel, f, f + 5 * n, f + 10 * n, f + 11 * n, n};
+  cudaEvent_t a = c->next_event(), b = c->next_event();
+  const int saved = c->ept;
+  double best_t = 1e300;
+  int best = saved;
+  for (int ept : candidates) {
+    c->ept = ept;
+    int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);  // warm-up
+    if (st) {
+      c->ept = saved;
+      return st;
+    }
+    cudaEventRecord(a, c->stream);
+    for (int rep = 0; rep < 2 && !st; ++rep) st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);
+    cudaEventRecord(b, c->stream);
+    if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
+    if (st) {
+      c->ept = saved;
+      return st;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_t) {
+      best_t = ms;
+      best = ept;
+    }
+  }
+  c->ev_used = 0;
+  c->ept = best;
+  if (best_ept) *best_ept = best;
+  if (best_events_per_s) *best_events_per_s = 2.0 * n * kBatch / (best_t * 1e-3);
   return TP_OK;
 }
 

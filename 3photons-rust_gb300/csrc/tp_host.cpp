@@ -611,11 +611,6 @@ D4 operator/(D4 a, D4 b) {
   for (int i = 0; i < 4; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) / (b.v * b.v);
   return r;
 }
-D4 dsqrt(D4 a) {
-  D4 r{std::sqrt(a.v), {}};
-  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] / (2.0 * r.v);
-  return r;
-}
 }  // namespace
 }  // namespace tp
 

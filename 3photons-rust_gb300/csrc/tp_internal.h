@@ -76,6 +76,25 @@ struct KParams {
   double* adj;               // adjoint: [n_batches][10] per-batch sums
 };
 
+// Batched form: many parameter points in one persistent launch. Work unit
+// u = one 10k batch of one point; units are numbered point by point.
+struct PointsParams {
+  const EvConst* points;            // [n_points]
+  const uint64_t* point_events;     // [n_points] events of each point's run
+  const uint64_t* point_unit0;      // [n_points] first unit of each point
+  const uint64_t* point_start;      // [n_points][4] xoshiro state at draw 0
+  const uint32_t* unit_point;       // [n_units]
+  const uint64_t* batch_table;      // 64 x 4: x^(12e4 * 2^k)
+  const uint64_t* thread_poly;      // x^(12 ept j)
+  uint64_t* unit_state;             // [n_units][4] scratch: batch start states
+  unsigned long long* counter;      // work-queue head, 0 at launch
+  unsigned long long* recheck_count;
+  BatchOut out;                     // stride n_units
+  uint64_t n_units;
+  int ept;
+  int precision;
+};
+
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
 constexpr int kMaxBins = 1024;
@@ -99,6 +118,8 @@ int launch_dump(int rng_kind, int precision, const EvConst& k, const uint64_t st
 
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
 int launch_binned(const KParams& p, int tpb, int grid, void* stream);
+int launch_points(const PointsParams& p, int tpb, void* stream);
+int points_grid(int precision, int tpb);  // persistent grid size on the current device
 int launch_adjoint(const KParams& p, int tpb, void* stream);
 
 }  // namespace tp

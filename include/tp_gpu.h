@@ -199,6 +199,30 @@ int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
  * reference, whose batches run on one CPU thread each. */
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
 
+/* ---- batched form: many parameter points --------------------------------
+ * No counterpart in the reference, which runs one configuration per process.
+ * Runs n_points complete runs, each with its own configuration (physics,
+ * cuts, couplings, num_events) and its own xoshiro256+ stream given by its
+ * raw state at draw 0 (starts[4 p .. 4 p + 3], e.g. from
+ * tp_xoshiro_state_at), in ONE persistent launch captured once in a CUDA
+ * graph and replayed while the shapes stay the same. Point p's batches are
+ * outputs [unit0[p], unit0[p + 1]) of the caller's host arrays (capacity =
+ * their length; unit0 has n_points + 1 entries). mode_flags may be
+ * TP_MODE_NO_PHOTON_SORTING. Merge and finalise each point's range with
+ * tp_merge_finalize. */
+int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
+                  const uint64_t *starts, int mode_flags, int precision,
+                  uint64_t *unit0, tp_batch_soa *out, uint64_t capacity);
+
+/* Autotuner: times the xoshiro event kernel of `precision` on the first
+ * `sample_batches` batches of cfg for each candidate events-per-thread
+ * (which fixes the block shape, ceil(10000 / ept) threads rounded to
+ * warps), keeps the fastest for this context (all later launches, including
+ * tp_run_points) and reports it. */
+int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,
+                uint64_t sample_batches, int *best_ept,
+                double *best_events_per_s);
+
 /* ---- binned observables and their adjoint ---------------------------------
  * No counterpart in the reference (its histogram settings `num_bins`/`plot`
  * are read but unused, src/config.rs:45-51, src/main.rs:122). Every kept

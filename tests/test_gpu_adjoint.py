@@ -90,17 +90,21 @@ def test_torch_autograd_function(setup):
     assert torch.allclose(theta.grad, torch.tensor(grad), rtol=1e-12)
 
 
-def test_gradient_fit_recovers_betas(setup):
-    # 200 gradient-ascent steps on (beta+, beta-) from a small offset of the
-    # model point beta+- = 0 (beta- = 0 is a stationary point: only beta-^2
-    # enters the weights, so |beta-| is what the data determine)
-    _, _, _, _, model = setup
-    theta = np.array([0.0, 0.05, 91.187, 2.49])
-    _, g0, _, _ = model.gradient(theta)
-    lr = 0.02 / max(np.abs(g0[:2]).max(), 1e-300)
-    m = np.zeros(2)
-    for _ in range(200):
-        _, g, _, _ = model.gradient(theta)
-        m = 0.8 * m + g[:2]
-        theta[:2] += lr * m / (1 + 0.0 * np.abs(m))
-    assert abs(theta[0] - 0.3) < 0.03 and abs(abs(theta[1]) - 0.2) < 0.03, theta
+def test_gradient_fit_recovers_betas(tp, ctx, cfg_sqrts1000):
+    # 200 natural-gradient steps (adjoint gradient, Gauss-Newton Fisher
+    # preconditioner) on (beta+, beta-) from near the model point beta+- = 0.
+    # Only beta-^2 enters the weights, so the data fix |beta-|; beta+ also
+    # enters linearly through the interference terms.
+    prec = tp.TP_PREC_FP32_MIXED
+    bins = tp.binning(20, 20)
+    data_cfg = cfg_sqrts1000.replace(num_events=20_000_000, beta_plus=0.3, beta_minus=-0.2)
+    data = ctx.binned_forward(data_cfg, 0, data_cfg.num_batches, bins, SEED_DATA, prec)
+    model_cfg = cfg_sqrts1000.replace(num_events=20_000_000, beta_plus=0.0, beta_minus=0.0)
+    model = tp.BinnedGaussianLikelihood(ctx, model_cfg, SEED_MODEL, model_cfg.num_batches, data, data_cfg, bins,
+                                        precision=prec)
+    theta, cov = tp.fit(model, [0.05, 0.05, 91.187, 2.49], steps=200, lr=0.5)
+    err = np.sqrt(np.diag(cov))
+    # statistical errors of data and model both enter (the likelihood only
+    # counts the data's): allow 5 of the Fisher errors, at least 0.02
+    tol = np.maximum(5 * np.sqrt(2) * err, 0.02)
+    assert abs(theta[0] - 0.3) < tol[0] and abs(abs(theta[1]) - 0.2) < tol[1], (theta, err)

@@ -1,0 +1,52 @@
+"""Batched form: many parameter points with uneven event counts in one
+persistent launch (captured in a CUDA graph), against the one-point path on
+the same streams, and the autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_points(tp, base, n=12, seed=5):
+    cfgs, _ = tp.scan_points(base, n, seed)
+    r = np.random.default_rng(seed)
+    # uneven, ragged sizes: from one event to a few batches
+    sizes = [1, 9999, 10000, 10001] + [int(x) for x in r.integers(1, 60_000, n - 4)]
+    cfgs = [c.replace(num_events=s) for c, s in zip(cfgs, sizes)]
+    seeds = [1000 + 7 * p for p in range(n)]
+    starts = [tp.xoshiro_start(s) for s in seeds]
+    return cfgs, seeds, starts
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32-mixed"])
+def test_points_match_one_point_path(tp, cfg_valeurs, precision):
+    cfgs, seeds, starts = small_points(tp, cfg_valeurs)
+    with tp.Context(0) as ctx:
+        parts = ctx.run_points(cfgs, starts, precision)
+        again = ctx.run_points(cfgs, starts, precision)  # graph replay
+        for cfg, seed, part, rep in zip(cfgs, seeds, parts, again):
+            ref = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", seed=seed, precision=precision)
+            for got in (part, rep):
+                assert np.array_equal(got.selected, ref.selected)
+                a, b = got.as_array()[:, 1:], ref.as_array()[:, 1:]
+                assert np.all(np.abs(a - b) <= 1e-12 * np.maximum(np.abs(b), 1e-300))
+
+
+def test_points_stream_is_jumped_seed(tp, oracle, cfg_sqrts1000):
+    # scan_points' point p starts from seed 12345 jumped p times by 2^128
+    # (the reference's faster-threading batch p), computed here by the
+    # polynomial jump and by the restatement's matrix squaring
+    _, starts = tp.scan_points(cfg_sqrts1000, 4)
+    for p in range(4):
+        assert [int(x) for x in starts[p]] == oracle.xoshiro_state(tp.XOSHIRO_DEFAULT_SEED, p)
+
+
+def test_autotune_keeps_results(tp, cfg_sqrts1000):
+    cfg = cfg_sqrts1000.replace(num_events=300_000)
+    with tp.Context(0) as ctx:
+        ref = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", precision=1)
+        ept, rate = ctx.autotune(cfg, 1, 512)
+        assert 40 <= ept <= 125 and rate > 1e9
+        got = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", precision=1)
+    assert np.array_equal(got.selected, ref.selected)
+    assert np.allclose(got.sigma, ref.sigma, rtol=1e-12)
