@@ -166,6 +166,7 @@ def library():
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
         "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
+        "tp_run_batches_noalloc": (i32, [P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
         "tp_run_points": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_uint64), i32, i32,
                                 P(ctypes.c_uint64), P(CBatchSoa), u64]),
         "tp_autotune": (i32, [vp, P(CConfig), i32, u64, P(ctypes.c_int), P(ctypes.c_double)]),

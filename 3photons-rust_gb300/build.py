@@ -42,7 +42,7 @@ def build(verbose=False, extra_nvcc=()):
     inc = ["-I", CSRC, "-I", os.path.join(HERE, "..", "include")]
     host_flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra"]
     jobs = []
-    for src in ("tp_kernels.cu",):
+    for src in ("tp_kernels.cu", "tp_noalloc.cu"):
         obj = os.path.join(BUILD, src + ".o")
         jobs.append([nvcc, "-c", os.path.join(CSRC, src), "-o", obj, "-O3", "-std=c++17", *ARCH,
                      "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v", *inc, *extra_nvcc])
@@ -57,7 +57,7 @@ def build(verbose=False, extra_nvcc=()):
             if o.strip():
                 print(o)
     objs = [os.path.join(BUILD, s + ".o")
-            for s in ("tp_kernels.cu", "tp_capi.cpp", "tp_host.cpp", "tp_rng.cpp")]
+            for s in ("tp_kernels.cu", "tp_noalloc.cu", "tp_capi.cpp", "tp_host.cpp", "tp_rng.cpp")]
     cudalib = ["-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart"]
     _run([nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, *cudalib])
     os.replace(LIB + ".tmp", LIB)

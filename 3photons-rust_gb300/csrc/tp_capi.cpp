@@ -17,6 +17,13 @@ using namespace tp;
 
 thread_local std::string g_create_error;
 
+}  // namespace
+
+namespace tp {
+void set_thread_error(const char* msg) { g_create_error = msg; }
+}  // namespace tp
+
+namespace {
 
 // Batches per launch: bounds the device scratch (batch start states) to
 // 64 Ki batches = 14.7 MB (ranf) or 2 MB (xoshiro).

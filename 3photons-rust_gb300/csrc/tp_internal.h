@@ -116,6 +116,8 @@ int launch_dump(int rng_kind, int precision, const EvConst& k, const uint64_t st
                 const uint32_t* d_ranf_table, uint64_t first_event, uint64_t n,
                 tp_event_dump* d_out, unsigned int* d_err, void* stream);
 
+// message returned by tp_last_error(NULL) on this thread
+void set_thread_error(const char* msg);
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
 int launch_binned(const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);

@@ -156,7 +156,8 @@ typedef struct tp_ctx tp_ctx;
 tp_ctx *tp_create(int device, int *status);
 void tp_destroy(tp_ctx *ctx);
 /* Message of the last failing call on `ctx` ("" if none). With ctx == NULL:
- * the message of the last failing tp_create on this thread. */
+ * the message of the last failing context-free call (tp_create,
+ * tp_run_batches_noalloc) on this thread. */
 const char *tp_last_error(const tp_ctx *ctx);
 
 /* Runs batches [first_batch, first_batch + n_batches) of a run configured by
@@ -294,6 +295,33 @@ int tp_xoshiro_state_at(uint64_t seed, uint64_t jumps128, uint64_t draws,
                         uint64_t state[4]);
 int tp_ranf_state_at(int32_t seed, uint64_t draws, int32_t slots[55],
                      int32_t *index);
+
+/* ---- allocation-free batches -----------------------------------------------
+ * No counterpart in the reference. For callers that must not allocate GPU
+ * memory when they want events: code running inside a CUDA graph capture,
+ * real-time or embedded hosts that plan all memory at start-up, programs
+ * whose GPU memory belongs to another allocator. Same work as
+ * tp_run_batches_async for the xoshiro256+ stream (rng_kind =
+ * TP_RNG_XOSHIRO256P, optionally with TP_MODE_* flags), FP64 or FP32-mixed,
+ * on the CURRENT CUDA device and the given stream (a cudaStream_t; NULL is
+ * the default stream), writing the caller's DEVICE arrays `out`. No context,
+ * no cudaMalloc/cudaFree: the working memory (the start state of each batch
+ * and the jump-ahead tables) lives in fixed arrays of the library, 140 KiB
+ * per GPU that loads the library, held until the process exits.
+ *  - at most TP_NOALLOC_MAX_BATCHES batches per call; larger ranges fail
+ *    with TP_ERR_INVALID: split them into several calls;
+ *  - the first call on a device sets that device up (looks up the arrays'
+ *    addresses, uploads the tables with a synchronous copy): make that
+ *    first call before any stream capture;
+ *  - every call shares the same working memory, so calls that overlap on
+ *    the GPU (other streams, other host threads) race; order them on one
+ *    stream or synchronise between them. Nothing in it needs clearing: each
+ *    call writes every entry it reads;
+ *  - errors: a negative TP_ERR_*, message in tp_last_error(NULL). */
+#define TP_NOALLOC_MAX_BATCHES 4096
+int tp_run_batches_noalloc(const tp_config *cfg, int rng_kind, uint64_t seed,
+                           uint64_t first_batch, uint64_t n_batches,
+                           int precision, tp_batch_soa *out, void *stream);
 
 /* ========================================================================
  * Host side kept from the reference (no GPU needed)
