@@ -648,6 +648,35 @@ def run_simulation_sharded(cfg, rank, world_size, run_batches, all_gather, **kw)
     return merge_finalize(cfg, BatchAccumulators.concatenate(parts))
 
 
+def run_simulation_resumable(cfg, checkpoint, run_batches, chunk_batches=1000):
+    """Checkpointed run: integrates the batches chunk by chunk and, after
+    every chunk, saves the per-batch sums so far to `checkpoint` (an .npz
+    path, written atomically). A restarted call resumes at the first missing
+    batch: batch b's stream is a pure function of (stream, seed, b), so the
+    resumed run equals an uninterrupted one bit for bit.
+    run_batches(first_batch, n) -> BatchAccumulators (e.g. a bound
+    Context.run_batches)."""
+    nb = cfg.num_batches
+    done = BatchAccumulators(0)
+    if os.path.exists(checkpoint):
+        with np.load(checkpoint) as z:
+            if int(z["num_events"]) != cfg.num_events:
+                raise ValueError("checkpoint belongs to another run")
+            done = BatchAccumulators.from_array(z["sums"])
+    parts = [done]
+    first = done.n
+    while first < nb:
+        n = min(chunk_batches, nb - first)
+        parts.append(run_batches(first, n))
+        first += n
+        acc = BatchAccumulators.concatenate(parts)
+        parts = [acc]
+        tmp = checkpoint + ".tmp.npz"
+        np.savez(tmp, sums=acc.as_array(), num_events=cfg.num_events)
+        os.replace(tmp, checkpoint)
+    return merge_finalize(cfg, BatchAccumulators.concatenate(parts))
+
+
 def dump_results(cfg, res, elapsed_seconds, directory=".", timestamp=None):
     """output::dump_results (src/output.rs:30-177): prints the report and
     writes res.times, res.data and appends pil.mc."""
