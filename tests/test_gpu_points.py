@@ -26,10 +26,16 @@ def test_points_match_one_point_path(tp, cfg_valeurs, precision):
         again = ctx.run_points(cfgs, starts, precision)  # graph replay
         for cfg, seed, part, rep in zip(cfgs, seeds, parts, again):
             ref = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", seed=seed, precision=precision)
+            # FP64: the tolerance of the batch tests; FP32-mixed: the two
+            # kernels may contract FP32 products differently (the counts,
+            # decided by the certified cuts, stay exact)
+            tol = 1e-12 if precision == 0 else 1e-5
             for got in (part, rep):
                 assert np.array_equal(got.selected, ref.selected)
                 a, b = got.as_array()[:, 1:], ref.as_array()[:, 1:]
-                assert np.all(np.abs(a - b) <= 1e-12 * np.maximum(np.abs(b), 1e-300))
+                scale = np.maximum(np.abs(b), np.abs(b[:, :1]))
+                assert np.all(np.abs(a - b) <= tol * np.maximum(scale, 1e-300))
+            assert rep.as_array().tobytes() == part.as_array().tobytes()  # graph replay is deterministic
 
 
 def test_points_stream_is_jumped_seed(tp, oracle, cfg_sqrts1000):
