@@ -71,6 +71,7 @@ struct tp_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   int ept = kDefaultEpt;
+  int occupancy = 2;  // FP32 xoshiro kernel variant: min CTAs per SM
   uint64_t* d_xo_batch = nullptr;
   uint64_t* d_xo_jump = nullptr;
   uint64_t* d_xo_draw = nullptr;
@@ -210,6 +211,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   kp.err = c->d_err;
   kp.recheck_count = c->d_recheck;
   kp.ept = c->ept;
+  kp.occupancy = c->occupancy;
   if (kind == TP_RNG_XOSHIRO256P) {
     if (int st = ensure_thread_poly(c, c->ept)) return st;
   } else if (!jpb) {
@@ -645,14 +647,19 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   auto* f = reinterpret_cast<double*>(sel + n);
   BatchOut o{sel, f, f + 5 * n, f + 10 * n, f + 11 * n, n};
   cudaEvent_t a = c->next_event(), b = c->next_event();
-  const int saved = c->ept;
+  const int saved = c->ept, saved_occ = c->occupancy;
   double best_t = 1e300;
-  int best = saved;
-  for (int ept : candidates) {
+  int best = saved, best_occ = saved_occ;
+  for (int cand = 0; cand < 2 * (int)(sizeof candidates / sizeof candidates[0]); ++cand) {
+    const int ept = candidates[cand >> 1];
+    const int occ = 2 + (cand & 1);
+    if (precision != TP_PREC_FP32_MIXED && occ != 2) continue;
     c->ept = ept;
+    c->occupancy = occ;
     int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);  // warm-up
     if (st) {
       c->ept = saved;
+      c->occupancy = saved_occ;
       return st;
     }
     cudaEventRecord(a, c->stream);
@@ -661,6 +668,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
     if (st) {
       c->ept = saved;
+      c->occupancy = saved_occ;
       return st;
     }
     float ms = 0.f;
@@ -668,10 +676,12 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     if (ms < best_t) {
       best_t = ms;
       best = ept;
+      best_occ = occ;
     }
   }
   c->ev_used = 0;
   c->ept = best;
+  c->occupancy = best_occ;
   if (best_ept) *best_ept = best;
   if (best_events_per_s) *best_events_per_s = 2.0 * n * kBatch / (best_t * 1e-3);
   return TP_OK;

@@ -218,8 +218,9 @@ int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
 /* Autotuner: times the xoshiro event kernel of `precision` on the first
  * `sample_batches` batches of cfg for each candidate events-per-thread
  * (which fixes the block shape, ceil(10000 / ept) threads rounded to
- * warps), keeps the fastest for this context (all later launches, including
- * tp_run_points) and reports it. */
+ * warps) and, for FP32-mixed, each kernel variant of 2 or 3 resident CTAs
+ * per SM; keeps the fastest for this context (all later launches, including
+ * tp_run_points) and reports its events per thread. */
 int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,
                 uint64_t sample_batches, int *best_ept,
                 double *best_events_per_s);
