@@ -640,7 +640,8 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   if (sample_batches == 0 || sample_batches > kChunk) return c->fail(TP_ERR_INVALID, "sample_batches out of range");
   cudaSetDevice(c->device);
   // events per thread -> threads per CTA = ceil(10000 / ept) rounded to warps
-  static const int candidates[] = {40, 42, 48, 56, 64, 80, 100, 125};
+  // (more events per thread: fewer per-thread stream jumps of 256 steps)
+  static const int candidates[] = {40, 50, 64, 80, 100, 125, 160, 200, 250};
   const size_t n = sample_batches;
   if (int st = ensure(c, &c->d_out, &c->out_bytes, n * 13 * 8, "output buffers")) return st;
   auto* sel = static_cast<uint64_t*>(c->d_out);

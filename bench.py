@@ -167,6 +167,9 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     ev32 = 10 * events
     nb = (ev32 + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
     cfg = workload_config(tp, ev32 * world)
+    # events per thread and kernel variant from the autotuner (first 2048
+    # batches of this workload)
+    tuned_ept, _ = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 2048)
     first32 = rank * nb
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)
     f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
@@ -197,6 +200,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     value = world * ev32 * args.steps / (sum(step_ms) * 1e-3)
     out = {"value": value, "unit": "events/s", "events_per_step": ev32 * world, "ms_per_step": sum(step_ms) / len(step_ms),
+           "autotuned_events_per_thread": tuned_ept,
            "kernel": "k_events_xoshiro_fp32", "kernel_ms": ev_ms / args.steps,
            "gpu_launches": int(ev_launches + seed_launches), "ratio_vs_fp64": None,
            "rechecked_fraction": rechecked / (ev32 * args.steps)}
@@ -363,6 +367,7 @@ def main():
             print(json.dumps(out))
         return
     costs = ctx.probe_fp64()
+    tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 2048)
 
     dev = torch.device("cuda", local)
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)
@@ -448,7 +453,8 @@ def main():
         "config": {"workload": "FP64 plain path, sqrt(s)=1000 GeV, xoshiro256+ seed 12345 with jump-ahead, "
                                "1e9 events = 1e5 batches of 1e4 per GPU",
                    "events_per_step": events * world, "batches": nb * world, "precision": "fp64",
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": "batch-range shards, no collective"},
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": "batch-range shards, no collective",
+                   "autotuned_events_per_thread": tuned_ept64},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "DFMA throughput measured in this run (tp_probe_fp64)",
