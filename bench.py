@@ -169,7 +169,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     cfg = workload_config(tp, ev32 * world)
     # events per thread and kernel variant from the autotuner (first 2048
     # batches of this workload)
-    tuned_ept, _ = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 2048)
+    tuned_ept = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 2048)[0] if not args.only else None
     first32 = rank * nb
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)
     f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
