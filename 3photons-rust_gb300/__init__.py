@@ -35,6 +35,7 @@ TP_RNG_RANF = 0
 TP_RNG_XOSHIRO256P = 1
 TP_MODE_JUMP_PER_BATCH = 0x100
 TP_MODE_NO_PHOTON_SORTING = 0x200
+TP_MODE_FASTER_EVGEN = 0x400
 TP_PREC_FP64 = 0
 TP_PREC_FP32_MIXED = 1
 RANF_DEFAULT_SEED = 234612947
@@ -252,12 +253,17 @@ class Configuration:
         return {f: getattr(self.c, f) for f in Configuration.FIELDS}
 
 
-def rng_flags(rng="ranf", jump_per_batch=False, sorting=True):
+def rng_flags(rng="ranf", jump_per_batch=False, sorting=True, faster_evgen=False):
+    """rng_kind of the C ABI for the reference's cargo features: rng
+    (`standard-random`), jump_per_batch (`multi-threading,faster-threading`),
+    sorting=False (`no-photon-sorting`), faster_evgen (`faster-evgen`)."""
     kind = {"ranf": TP_RNG_RANF, "xoshiro": TP_RNG_XOSHIRO256P, "standard-random": TP_RNG_XOSHIRO256P}[rng]
     if jump_per_batch:
         kind |= TP_MODE_JUMP_PER_BATCH
     if not sorting:
         kind |= TP_MODE_NO_PHOTON_SORTING
+    if faster_evgen:
+        kind |= TP_MODE_FASTER_EVGEN
     return kind
 
 
@@ -406,22 +412,24 @@ class Context:
         return n.value
 
     def run_batches(self, cfg, first_batch, n_batches, rng="ranf", seed=None, jump_per_batch=False, sorting=True,
-                    precision=TP_PREC_FP64, out=None):
+                    precision=TP_PREC_FP64, out=None, faster_evgen=False):
         """Per-batch accumulators of batches [first_batch, first_batch + n)."""
         seed = default_seed(rng) if seed is None else seed
         acc = out if out is not None else BatchAccumulators(n_batches)
         soa = acc.soa()
-        self.check(library().tp_run_batches(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+        flags = rng_flags(rng, jump_per_batch, sorting, faster_evgen)
+        self.check(library().tp_run_batches(self.h, ctypes.byref(cfg.c), flags,
                                             seed, first_batch, n_batches, precision, ctypes.byref(soa)))
         return acc
 
     def run_batches_device(self, cfg, first_batch, n_batches, out_ptrs, stream=0, rng="ranf", seed=None,
-                           jump_per_batch=False, sorting=True, precision=TP_PREC_FP64):
+                           jump_per_batch=False, sorting=True, precision=TP_PREC_FP64, faster_evgen=False):
         """Queues the batches on `stream` writing DEVICE arrays given as five
         raw pointers (selected, spm2, vars, sigma, variance)."""
         seed = default_seed(rng) if seed is None else seed
         soa = CBatchSoa(*[ctypes.c_void_p(p) for p in out_ptrs])
-        self.check(library().tp_run_batches_async(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting),
+        flags = rng_flags(rng, jump_per_batch, sorting, faster_evgen)
+        self.check(library().tp_run_batches_async(self.h, ctypes.byref(cfg.c), flags,
                                                   seed, first_batch, n_batches, precision, ctypes.byref(soa),
                                                   ctypes.c_void_p(stream)))
 
@@ -618,13 +626,14 @@ def fit(model, theta0, steps=200, lr=0.5, free=(0, 1), damping=1e-3):
 
 
 def run_simulation(cfg, rng="ranf", seed=None, jump_per_batch=False, sorting=True, precision=TP_PREC_FP64,
-                   device=0, ctx=None):
+                   device=0, ctx=None, faster_evgen=False):
     """scheduling::run_simulation (src/scheduling/mod.rs:31-59): every batch
     on the GPU, merged in batch order on the host, finalised."""
     own = ctx is None
     ctx = ctx or Context(device)
     try:
-        acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng, seed, jump_per_batch, sorting, precision)
+        acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng, seed, jump_per_batch, sorting, precision,
+                              faster_evgen=faster_evgen)
     finally:
         if own:
             ctx.close()

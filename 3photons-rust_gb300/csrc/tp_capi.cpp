@@ -33,6 +33,8 @@ constexpr int kDefaultEpt = 40;  // xoshiro: events per thread (250 x 40)
 
 struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
+  std::vector<uint64_t> xo_fe_chunk;                  // 64 x 4: x^(kFeChunk 2^k)
+  std::vector<uint64_t> xo_fe_lane;                   // 32 x 4: x^(kFeLaneSpan l)
   std::vector<uint32_t> ranf;                         // 64 x 55
 };
 
@@ -53,6 +55,19 @@ const Tables& host_tables() {
       pb = gf2_mulmod(pb, pb);
       pj = gf2_mulmod(pj, pj);
       pd = gf2_mulmod(pd, pd);
+    }
+    t.xo_fe_chunk.resize(256);
+    Gf2Poly pc = gf2_xpow(kFeChunk);
+    for (int k = 0; k < 64; ++k) {
+      for (int w = 0; w < 4; ++w) t.xo_fe_chunk[4 * k + w] = pc.w[w];
+      pc = gf2_mulmod(pc, pc);
+    }
+    t.xo_fe_lane.resize(128);
+    const Gf2Poly lane_step = gf2_xpow(kFeLaneSpan);
+    Gf2Poly cur{{1, 0, 0, 0}};
+    for (int l = 0; l < 32; ++l) {
+      for (int w = 0; w < 4; ++w) t.xo_fe_lane[4 * l + w] = cur.w[w];
+      cur = gf2_mulmod(cur, lane_step);
     }
     t.ranf.resize(64 * 55);
     RanfPoly r = ranf_xpow(55);
@@ -90,6 +105,17 @@ struct tp_ctx {
   double* d_hist = nullptr;   // binned forward: kMaxBins x kBinStride
   double* d_binw = nullptr;   // adjoint: bin weights (kMaxBins)
   double* d_adj = nullptr;    // adjoint: per-batch sums, kChunk x 10
+  // faster-evgen: jump tables, chunk list, chunk states, chunk maps, thread start states
+  uint64_t* d_xo_fe_chunk = nullptr;
+  uint64_t* d_xo_fe_lane = nullptr;
+  void* d_fe_chunks = nullptr;
+  size_t fe_chunks_bytes = 0;
+  void* d_fe_cstate = nullptr;
+  size_t fe_cstate_bytes = 0;
+  void* d_fe_map = nullptr;
+  size_t fe_map_bytes = 0;
+  void* d_fe_tstate = nullptr;
+  size_t fe_tstate_bytes = 0;
   int sms = 0;
   // batched form (tp_run_points): device buffers and the captured graph
   struct Points {
@@ -171,11 +197,13 @@ int ensure_ranf_window(tp_ctx* c, int32_t seed) {
   return st;
 }
 
-int check_kind(tp_ctx* c, int rng_kind) {
+int check_kind(tp_ctx* c, int rng_kind, bool faster_evgen_ok = false) {
   const int kind = rng_kind & TP_RNG_KIND_MASK;
   if (kind != TP_RNG_RANF && kind != TP_RNG_XOSHIRO256P) return c->fail(TP_ERR_INVALID, "unknown rng kind");
-  if (rng_kind & ~(TP_RNG_KIND_MASK | TP_MODE_JUMP_PER_BATCH | TP_MODE_NO_PHOTON_SORTING))
+  if (rng_kind & ~(TP_RNG_KIND_MASK | TP_MODE_JUMP_PER_BATCH | TP_MODE_NO_PHOTON_SORTING | TP_MODE_FASTER_EVGEN))
     return c->fail(TP_ERR_INVALID, "unknown mode flag");
+  if ((rng_kind & TP_MODE_FASTER_EVGEN) && !faster_evgen_ok)
+    return c->fail(TP_ERR_UNSUPPORTED, "TP_MODE_FASTER_EVGEN is served by tp_run_batches and tp_run_batches_async only");
   return TP_OK;
 }
 
@@ -187,6 +215,9 @@ int check_seed(tp_ctx* c, int rng_kind, uint64_t seed) {
 
 enum class Pass { kBatches, kBinned, kAdjoint };
 
+int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+           int precision, const BatchOut& out, cudaStream_t stream);
+
 // Queues the batches on `stream`; `out` holds device pointers (stride n).
 // `pass` selects the per-batch accumulators, the binned forward pass or the
 // adjoint pass (the latter two take their extra fields from `extra`).
@@ -195,13 +226,15 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
               Pass pass = Pass::kBatches, const KParams* extra = nullptr,
               std::vector<double>* adj_host = nullptr) {
   if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
-  if (int st = check_kind(c, rng_kind)) return st;
+  if (int st = check_kind(c, rng_kind, pass == Pass::kBatches)) return st;
   if (int st = check_seed(c, rng_kind, seed)) return st;
   if (n_batches == 0) return TP_OK;
   if (first_batch > (1ull << 46) || n_batches > (1ull << 46))
     return c->fail(TP_ERR_INVALID, "batch range too large");
   if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
     return c->fail(TP_ERR_INVALID, "unknown precision");
+  if (rng_kind & TP_MODE_FASTER_EVGEN)
+    return run_fe(c, cfg, rng_kind, seed, first_batch, n_batches, precision, out, stream);
   const int kind = rng_kind & TP_RNG_KIND_MASK;
   const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
   KParams kp{};
@@ -287,6 +320,204 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   return TP_OK;
 }
 
+// ---------------------------------------------------------------------------
+// faster-evgen (TP_MODE_FASTER_EVGEN). The draws per event vary, so every
+// event's first draw is found before the physics:
+//  1. map pass: per chunk of kFeChunk draw positions, for 32 entry offsets,
+//     the offset where the chunk's last event ends and the chunk's event
+//     count (k_fe_map, one warp per chunk, from the accept bits);
+//  2. on the host, the maps composed along each stream from draw 0: the
+//     first event and its offset in every chunk;
+//  3. starts pass: per chunk, the stream state at each thread's first event
+//     (k_fe_starts);
+//  4. the event kernel, one CTA per batch (k_fe_events_fp64).
+// One stream (events numbered through the run) or one per batch
+// (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
+// ---------------------------------------------------------------------------
+constexpr uint64_t kFeMapLaunch = 16384;  // chunks per map launch
+constexpr uint64_t kFePiece = 4096;       // batches per starts + events launch
+
+struct FeStream {
+  uint64_t id = 0;       // 0, or the batch for per-batch streams
+  uint64_t target = 0;   // events whose chunk must be known
+  uint64_t next_chunk = 0;
+  uint64_t events = 0;   // events starting before chunk next_chunk
+  uint32_t entry = 0;    // offset of chunk next_chunk's first event
+  std::vector<FeChunk> chunks;  // composed chunks (entry, first_event)
+  bool done() const { return events >= target; }
+};
+
+// Uploads `descs`, seeds their chunk states and runs `pass` on them.
+int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool map_pass, cudaStream_t stream,
+              std::vector<uint32_t>* maps) {
+  const size_t n = descs.size();
+  if (n == 0) return TP_OK;
+  if (int st = ensure(c, &c->d_fe_chunks, &c->fe_chunks_bytes, n * sizeof(FeChunk), "faster-evgen chunks")) return st;
+  if (int st = ensure(c, &c->d_fe_cstate, &c->fe_cstate_bytes, n * 56 * sizeof(int32_t), "faster-evgen chunk states"))
+    return st;
+  if (map_pass)
+    if (int st = ensure(c, &c->d_fe_map, &c->fe_map_bytes, n * kFeEntries * sizeof(uint32_t), "faster-evgen maps"))
+      return st;
+  int st = c->cuda(cudaMemcpyAsync(c->d_fe_chunks, descs.data(), n * sizeof(FeChunk), cudaMemcpyHostToDevice, stream),
+                   "upload faster-evgen chunks");
+  if (st) return st;
+  fp.chunks = static_cast<const FeChunk*>(c->d_fe_chunks);
+  fp.n_chunks = n;
+  fp.chunk_state = c->d_fe_cstate;
+  fp.map = static_cast<uint32_t*>(c->d_fe_map);
+  if (launch_fe_seed(fp, stream) != TP_OK)
+    return c->fail(TP_ERR_CUDA, std::string("faster-evgen seed launch: ") + cudaGetErrorString(cudaGetLastError()));
+  if ((map_pass ? launch_fe_map(fp, stream) : launch_fe_starts(fp, stream)) != TP_OK)
+    return c->fail(TP_ERR_CUDA, std::string("faster-evgen chunk launch: ") + cudaGetErrorString(cudaGetLastError()));
+  if (!map_pass) return TP_OK;
+  maps->resize(n * kFeEntries);
+  st = c->cuda(cudaMemcpyAsync(maps->data(), c->d_fe_map, n * kFeEntries * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               stream), "copy faster-evgen maps");
+  if (!st) st = c->cuda(cudaStreamSynchronize(stream), "faster-evgen map pass");
+  return st;
+}
+
+// Steps 1-2 for `streams`: composes chunks until each stream's target.
+int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cudaStream_t stream) {
+  std::vector<FeChunk> descs;
+  std::vector<uint32_t> maps, one;
+  for (;;) {
+    descs.clear();
+    for (FeStream& s : streams) {
+      if (s.done()) continue;
+      // ~16.6 (xoshiro) or ~17.9 (ranf, block skips) draws per event; two chunks of slack
+      const uint64_t need = (uint64_t)((double)(s.target - s.events) * 18.5 / kFeChunk) + 2;
+      for (uint64_t k = 0; k < need && descs.size() < kFeMapLaunch; ++k)
+        descs.push_back(FeChunk{s.id, s.next_chunk + k, 0, 0, 0});
+      if (descs.size() >= kFeMapLaunch) break;
+    }
+    if (descs.empty()) return TP_OK;
+    if (int st = fe_launch(c, fp, descs, true, stream, &maps)) return st;
+    size_t d = 0;
+    for (FeStream& s : streams) {
+      while (d < descs.size() && descs[d].stream == s.id && descs[d].chunk == s.next_chunk && !s.done()) {
+        uint32_t m;
+        if (s.entry < (uint32_t)kFeEntries) {
+          m = maps[d * kFeEntries + s.entry];
+        } else {  // the chunk is entered past the 32 mapped offsets: map that offset alone
+          std::vector<FeChunk> single{FeChunk{s.id, s.next_chunk, 0, s.entry, 0}};
+          if (int st = fe_launch(c, fp, single, true, stream, &one)) return st;
+          m = one[0];
+        }
+        if (m == kFeMapError)
+          return c->fail(TP_ERR_DEVICE, "faster-evgen: an event runs past its chunk's accept bits");
+        s.chunks.push_back(FeChunk{s.id, s.next_chunk, s.events, s.entry, 0});
+        s.events += m & 0xffffu;
+        s.entry = m >> 16;
+        ++s.next_chunk;
+        ++d;
+      }
+      while (d < descs.size() && descs[d].stream == s.id) ++d;  // maps past the target
+    }
+  }
+}
+
+int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+           int precision, const BatchOut& out, cudaStream_t stream) {
+  if (precision != TP_PREC_FP64)
+    return c->fail(TP_ERR_UNSUPPORTED, "TP_MODE_FASTER_EVGEN runs in FP64 only");
+  const int kind = rng_kind & TP_RNG_KIND_MASK;
+  const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
+  const uint64_t n_total = cfg->num_events;
+  FeParams fp{};
+  fp.kind = kind;
+  fp.jpb = jpb;
+  fp.err = c->d_err;
+  fp.ept = c->ept;
+  const int tpb = (((kBatch + c->ept - 1) / c->ept) + 31) / 32 * 32;
+  fp.tpb = tpb;
+  fp.num_events = n_total;
+  if (kind == TP_RNG_XOSHIRO256P) {
+    xoshiro_seed(seed, fp.xo_start);
+  } else {
+    fp.ranf_seed = (int32_t)seed;
+    if (!jpb)
+      if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
+  }
+  fp.ranf_window = c->d_ranf_window;
+  fp.ranf_table = c->d_ranf_tab;
+  fp.xo_stream = c->d_xo_jump;
+  fp.xo_chunk = c->d_xo_fe_chunk;
+  fp.xo_lane = c->d_xo_fe_lane;
+  KParams kp{};
+  make_ev_const(*cfg, rng_kind & ~TP_RNG_KIND_MASK, &kp.k);
+  kp.num_events = n_total;
+  kp.precision = precision;
+  kp.err = c->d_err;
+  kp.ept = c->ept;
+  const size_t state_bytes = kind == TP_RNG_RANF ? 56 * sizeof(int32_t) : 4 * sizeof(uint64_t);
+  const uint64_t b_end = first_batch + n_batches;
+  // one stream: compose once through the last event of the range
+  std::vector<FeStream> one(1);
+  if (!jpb) {
+    // batches past the run are empty: their event kernel CTAs store zeros
+    const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
+    one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
+    if (int st = fe_compose(c, fp, one, stream)) return st;
+  }
+  for (uint64_t p0 = first_batch; p0 < b_end; p0 += kFePiece) {
+    const uint64_t pn = b_end - p0 < kFePiece ? b_end - p0 : kFePiece;
+    std::vector<FeChunk> descs;
+    if (!jpb) {
+      const uint64_t lo = p0 * (uint64_t)kBatch;
+      const uint64_t hi = (p0 + pn) * (uint64_t)kBatch;
+      const std::vector<FeChunk>& ch = one[0].chunks;
+      for (size_t k = 0; k < ch.size(); ++k) {
+        const uint64_t f0 = ch[k].first_event;
+        const uint64_t f1 = k + 1 < ch.size() ? ch[k + 1].first_event : one[0].events;
+        if (f0 < hi && f1 > lo && f1 > f0) descs.push_back(ch[k]);
+      }
+    } else {
+      std::vector<FeStream> streams(pn);
+      for (uint64_t i = 0; i < pn; ++i) {
+        streams[i].id = p0 + i;
+        const uint64_t lo = (p0 + i) * (uint64_t)kBatch;
+        streams[i].target = lo >= n_total ? 0 : (n_total - lo < (uint64_t)kBatch ? n_total - lo : kBatch);
+      }
+      if (int st = fe_compose(c, fp, streams, stream)) return st;
+      for (const FeStream& s : streams) descs.insert(descs.end(), s.chunks.begin(), s.chunks.end());
+    }
+    if (int st = ensure(c, &c->d_fe_tstate, &c->fe_tstate_bytes, (size_t)pn * tpb * state_bytes,
+                        "faster-evgen thread states"))
+      return st;
+    FeParams sp = fp;
+    sp.first_batch = p0;
+    sp.n_batches = pn;
+    sp.thread_state = c->d_fe_tstate;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
+    if (int st = fe_launch(c, sp, descs, false, stream, nullptr)) return st;
+    if (e1) {
+      cudaEventRecord(e1, stream);
+      c->prof_marks.push_back({0, {e0, e1}});
+      e0 = e1 = nullptr;
+    }
+    const uint64_t off = p0 - first_batch;
+    kp.first_batch = p0;
+    kp.n_batches = pn;
+    kp.batch_state = c->d_fe_tstate;
+    kp.out = out;
+    kp.out.selected = out.selected + off;
+    kp.out.spm2 = out.spm2 + off;
+    kp.out.vars = out.vars + off;
+    kp.out.sigma = out.sigma + off;
+    kp.out.variance = out.variance + off;
+    if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
+    const int st = launch_fe_events(rng_kind, kp, tpb, stream);
+    if (e1) {
+      cudaEventRecord(e1, stream);
+      c->prof_marks.push_back({1, {e0, e1}});
+    }
+    if (st) return c->fail(st, std::string("faster-evgen event launch: ") + cudaGetErrorString(cudaGetLastError()));
+  }
+  return TP_OK;
+}
+
 int binning_params(tp_ctx* c, const tp_config* cfg, const tp_binning* bins, KParams* kp) {
   if (!bins || bins->n_emax < 1 || bins->n_cos < 1 || (int64_t)bins->n_emax * bins->n_cos > kMaxBins)
     return c->fail(TP_ERR_INVALID, "binning: 1 <= n_emax * n_cos <= 1024");
@@ -344,6 +575,8 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_hist, kMaxBins * kBinStride * sizeof(double), "histogram");
   alloc((void**)&c->d_binw, kMaxBins * sizeof(double), "bin weights");
   alloc((void**)&c->d_adj, kChunk * 10 * sizeof(double), "adjoint sums");
+  alloc((void**)&c->d_xo_fe_chunk, 256 * 8, "tables");
+  alloc((void**)&c->d_xo_fe_lane, 128 * 8, "tables");
   if (!st) st = c->cuda(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "device query");
   alloc(&c->d_state, kChunk * 56 * 4, "batch states");
   (void)dummy;
@@ -352,6 +585,9 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_jump, t.xo_jump.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_draw, t.xo_draw.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), 64 * 55 * 4, cudaMemcpyHostToDevice), "tables");
+  if (!st)
+    st = c->cuda(cudaMemcpy(c->d_xo_fe_chunk, t.xo_fe_chunk.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st) st = c->cuda(cudaMemcpy(c->d_xo_fe_lane, t.xo_fe_lane.data(), 128 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
   if (!st) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof(unsigned long long)), "recheck counter");
   if (st) {
@@ -370,7 +606,8 @@ void tp_destroy(tp_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly,
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
-                  c->d_hist, c->d_binw, c->d_adj};
+                  c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
+                  c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);

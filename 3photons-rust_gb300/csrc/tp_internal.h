@@ -96,6 +96,58 @@ struct PointsParams {
   int precision;
 };
 
+// faster-evgen (src/evgen.rs:143-173, 221-249): an event takes 15 draws plus
+// 2 per rejected point, so event boundaries are found before the physics.
+// A stream's draw positions are cut into chunks of kFeChunk; an event
+// belongs to the chunk of its first draw. One warp per chunk computes the
+// accept bits of kFeSpan positions (the chunk and a margin for the events
+// that run past its end), 1152 per lane.
+constexpr uint32_t kFeChunk = 32768;
+constexpr uint32_t kFeSpan = 36864;
+constexpr uint32_t kFeLaneSpan = kFeSpan / 32;
+constexpr int kFeEntries = 32;             // entry offsets per chunk map
+constexpr uint32_t kFeMapError = 0xffffffffu;
+constexpr int kFeMaxStarts = 128;          // thread starts recorded per chunk
+constexpr int kFeMaxTries = 2048;          // re-rolls per point (the span holds fewer)
+// error bits set by the faster-evgen kernels
+constexpr unsigned kFeErrSpan = 0x10u;     // an event ran past the chunk's span
+constexpr unsigned kFeErrStarts = 0x20u;   // too many thread starts in a chunk
+constexpr unsigned kFeErrTries = 0x40u;    // a point was re-rolled kFeMaxTries times
+
+// One chunk of a stream: for the map pass, lane l chases entry offset
+// entry + l; for the starts pass, entry is the offset of the chunk's first
+// event and first_event its index within the stream.
+struct FeChunk {
+  uint64_t stream;  // one-stream runs: 0; per-batch streams: the batch
+  uint64_t chunk;   // positions [chunk * kFeChunk, ...) of the stream
+  uint64_t first_event;
+  uint32_t entry;
+  uint32_t pad;
+};
+
+struct FeParams {
+  int kind;                      // TP_RNG_RANF or TP_RNG_XOSHIRO256P
+  int jpb;                       // per-batch streams (TP_MODE_JUMP_PER_BATCH)
+  uint64_t xo_start[4];          // xoshiro state at draw 0 of the seed
+  int32_t ranf_seed;
+  const int32_t* ranf_window;    // one-stream ranf: blocks 0 and 1 of the stream
+  const uint32_t* ranf_table;    // x^(55 2^k) mod P
+  const uint64_t* xo_stream;     // x^(2^128 2^k): per-batch stream starts
+  const uint64_t* xo_chunk;      // x^(kFeChunk 2^k)
+  const uint64_t* xo_lane;       // x^(kFeLaneSpan l), l < 32
+  const FeChunk* chunks;
+  uint64_t n_chunks;
+  void* chunk_state;             // per chunk: xoshiro 4 x u64, ranf 56 x i32
+  uint32_t* map;                 // map pass: [n_chunks][32] exit << 16 | events
+  // starts pass: thread t of batch first_batch + i starts event
+  // kBatch (first_batch + i) + ept t; its stream state goes to
+  // thread_state[i * tpb + t] (xoshiro 4 x u64, ranf 56 x i32)
+  uint64_t first_batch, n_batches, num_events;
+  int ept, tpb;
+  void* thread_state;
+  unsigned int* err;
+};
+
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
 constexpr int kMaxBins = 1024;
@@ -124,6 +176,12 @@ int launch_binned(const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);
 int points_grid(int precision, int tpb);  // persistent grid size on the current device
 int launch_adjoint(const KParams& p, int tpb, void* stream);
+// faster-evgen passes: chunk start states, chunk maps, thread start states,
+// events (batch_state = the thread start states)
+int launch_fe_seed(const FeParams& p, void* stream);
+int launch_fe_map(const FeParams& p, void* stream);
+int launch_fe_starts(const FeParams& p, void* stream);
+int launch_fe_events(int rng_kind, const KParams& p, int tpb, void* stream);
 
 }  // namespace tp
 

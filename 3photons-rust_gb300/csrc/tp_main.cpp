@@ -5,7 +5,7 @@
 //
 // usage: tp_run [-c valeurs] [-d output dir] [-n num_events] [--device D]
 //               [--rng ranf|xoshiro] [--seed S] [--jump-per-batch]
-//               [--no-photon-sorting] [--fp32-mixed]
+//               [--no-photon-sorting] [--faster-evgen] [--fp32-mixed]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -38,6 +38,7 @@ int main(int argc, char** argv) {
     else if (a == "--seed") { seed = std::strtoull(next(), nullptr, 10); seed_given = true; }
     else if (a == "--jump-per-batch") flags |= TP_MODE_JUMP_PER_BATCH;
     else if (a == "--no-photon-sorting") flags |= TP_MODE_NO_PHOTON_SORTING;
+    else if (a == "--faster-evgen") flags |= TP_MODE_FASTER_EVGEN;
     else if (a == "--fp32-mixed") precision = TP_PREC_FP32_MIXED;
     else {
       std::fprintf(stderr, "unknown argument %s\n", a.c_str());

@@ -73,12 +73,21 @@ extern "C" {
  * wrapping arithmetic, ranf.rs:137-140; xoshiro: b jumps of 2^128 draws,
  * standard.rs:53-55).
  * TP_MODE_NO_PHOTON_SORTING reproduces `--features no-photon-sorting`
- * (src/evgen.rs:109, src/event.rs:96-105). */
+ * (src/evgen.rs:109, src/event.rs:96-105).
+ * TP_MODE_FASTER_EVGEN reproduces `--features faster-evgen`
+ * (src/evgen.rs:143-173, 221-249): 9 + 6 draws per event as random_array
+ * blocks, plus 2 per re-rolled unit-circle point, so the draws per event
+ * vary. The library first finds every event's first draw (a pass over the
+ * stream's accept bits from draw 0, also for first_batch > 0), then runs the
+ * events. FP64 only (TP_PREC_FP32_MIXED gives TP_ERR_UNSUPPORTED), batch
+ * accumulators only (tp_run_batches / tp_run_batches_async); the _async call
+ * waits for the boundary pass before it queues the event kernels. */
 #define TP_RNG_RANF 0
 #define TP_RNG_XOSHIRO256P 1
 #define TP_RNG_KIND_MASK 0xff
 #define TP_MODE_JUMP_PER_BATCH 0x100
 #define TP_MODE_NO_PHOTON_SORTING 0x200
+#define TP_MODE_FASTER_EVGEN 0x400
 
 #define TP_RANF_DEFAULT_SEED 234612947ull
 #define TP_XOSHIRO_DEFAULT_SEED 12345ull

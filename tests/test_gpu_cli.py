@@ -15,7 +15,8 @@ CLI = os.path.join(ROOT, "3photons-rust_gb300", "tp_run")
 
 
 @pytest.mark.parametrize("features,args", [("", []), ("standard-random", ["--rng", "xoshiro"]),
-                                           ("multi-threading,faster-threading", ["--jump-per-batch"])])
+                                           ("multi-threading,faster-threading", ["--jump-per-batch"]),
+                                           ("faster-evgen", ["--faster-evgen"])])
 def test_tp_run_reproduces_golden(tmp_path, features, args):
     out = subprocess.run([CLI, "-c", os.path.join(GOLDEN, "valeurs"), "-d", str(tmp_path), *args],
                          capture_output=True, text=True, check=True).stdout
