@@ -335,7 +335,9 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
 constexpr uint64_t kFeMapLaunch = 16384;  // chunks per map launch
-constexpr uint64_t kFePiece = 4096;       // batches per starts + events launch
+// batches per starts + events launch: bounds the thread start states to
+// 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
+constexpr uint64_t kFePieceXo = 16384, kFePieceRanf = 4096;
 
 struct FeStream {
   uint64_t id = 0;       // 0, or the batch for per-batch streams
@@ -460,8 +462,9 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }
-  for (uint64_t p0 = first_batch; p0 < b_end; p0 += kFePiece) {
-    const uint64_t pn = b_end - p0 < kFePiece ? b_end - p0 : kFePiece;
+  const uint64_t piece = kind == TP_RNG_RANF ? kFePieceRanf : kFePieceXo;
+  for (uint64_t p0 = first_batch; p0 < b_end; p0 += piece) {
+    const uint64_t pn = b_end - p0 < piece ? b_end - p0 : piece;
     std::vector<FeChunk> descs;
     if (!jpb) {
       const uint64_t lo = p0 * (uint64_t)kBatch;

@@ -255,6 +255,42 @@ def grad_leg(tp, ctx, args, events):
             "max_rel_dev_vs_analytic": float(np.max(np.abs(grad - ga)) / np.max(np.abs(ga)))}
 
 
+def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=None):
+    """`--features faster-evgen` (TP_MODE_FASTER_EVGEN), FP64, one stream:
+    the boundary pass (chunk maps, host composition, thread start states)
+    plus the event kernel, timed on the device around the whole call."""
+    cfg = workload_config(tp, events)
+    nb = (events + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
+    sel = torch.zeros(nb, dtype=torch.int64, device=dev)
+    f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
+    ptrs = [sel.data_ptr(), f.data_ptr(), f.data_ptr() + 5 * nb * 8, f.data_ptr() + 10 * nb * 8,
+            f.data_ptr() + 11 * nb * 8]
+
+    def step():
+        ctx.run_batches_device(cfg, 0, nb, ptrs, stream=stream.cuda_stream, rng=rng, seed=seed, faster_evgen=True)
+
+    step()
+    torch.cuda.synchronize()
+    steps = 2
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.profile(True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        for _ in range(steps):
+            step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    ev_ms, _, _, _ = ctx.profile_read()
+    ctx.profile(False)
+    ms = a.elapsed_time(b) / steps
+    out = {"rng": rng, "events": events, "ms_per_step": ms, "events_per_s": events / (ms * 1e-3),
+           "event_kernel_ms": ev_ms / steps, "boundary_pass_ms": ms - ev_ms / steps,
+           "selected": int(sel.sum().item())}
+    if fp64_value:
+        out["vs_default_evgen_fp64"] = out["events_per_s"] / fp64_value
+    return out
+
+
 def points_leg(tp, ctx, args):
     """The batched form: 256 parameter points (sqrt(s) ~ U[200, 2000] GeV,
     E_min ~ U[1, 50] GeV, |cos| cuts ~ U[0.80, 0.99], beta+- ~ U[-1, 1],
@@ -333,7 +369,7 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--events", type=int, default=WORKLOAD_EVENTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["fp64", "fp32"], default=None,
+    ap.add_argument("--only", choices=["fp64", "fp32", "fe"], default=None,
                     help="time one leg only (no e2e, no CPU baseline): for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -363,6 +399,14 @@ def main():
     if args.only == "fp32":
         out = fp32_leg(tp, ctx, torch, torch.device("cuda", local), torch.cuda.Stream(torch.device("cuda", local)),
                        args, events // 10, world, rank, None, None, None, 0, 0)
+        if rank == 0:
+            print(json.dumps(out))
+        return
+    if args.only == "fe":
+        dev = torch.device("cuda", local)
+        st = torch.cuda.Stream(dev)
+        out = [faster_evgen_leg(tp, ctx, torch, dev, st, events, "xoshiro", SEED),
+               faster_evgen_leg(tp, ctx, torch, dev, st, events // 5, "ranf", tp.RANF_DEFAULT_SEED)]
         if rank == 0:
             print(json.dumps(out))
         return
@@ -470,6 +514,9 @@ def main():
     if world == 1:
         line["grad"] = grad_leg(tp, ctx, args, events)
         line["batched"] = points_leg(tp, ctx, args)
+        line["faster_evgen"] = [faster_evgen_leg(tp, ctx, torch, dev, stream, events, "xoshiro", SEED, value),
+                                faster_evgen_leg(tp, ctx, torch, dev, stream, events // 5, "ranf",
+                                                 tp.RANF_DEFAULT_SEED)]
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(tp)
     print(json.dumps(line))
