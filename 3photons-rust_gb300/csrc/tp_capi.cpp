@@ -86,7 +86,7 @@ struct tp_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   int ept = kDefaultEpt;
-  int occupancy = 2;  // FP32 xoshiro kernel variant: min CTAs per SM
+  int occupancy[2] = {2, 2};  // xoshiro event kernel variant per precision: min CTAs per SM
   uint64_t* d_xo_batch = nullptr;
   uint64_t* d_xo_jump = nullptr;
   uint64_t* d_xo_draw = nullptr;
@@ -244,7 +244,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   kp.err = c->d_err;
   kp.recheck_count = c->d_recheck;
   kp.ept = c->ept;
-  kp.occupancy = c->occupancy;
+  kp.occupancy = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
   if (kind == TP_RNG_XOSHIRO256P) {
     if (int st = ensure_thread_poly(c, c->ept)) return st;
   } else if (!jpb) {
@@ -888,19 +888,19 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   auto* f = reinterpret_cast<double*>(sel + n);
   BatchOut o{sel, f, f + 5 * n, f + 10 * n, f + 11 * n, n};
   cudaEvent_t a = c->next_event(), b = c->next_event();
-  const int saved = c->ept, saved_occ = c->occupancy;
+  const int pi = precision == TP_PREC_FP32_MIXED ? 1 : 0;
+  const int saved = c->ept, saved_occ = c->occupancy[pi];
   double best_t = 1e300;
   int best = saved, best_occ = saved_occ;
   for (int cand = 0; cand < 2 * (int)(sizeof candidates / sizeof candidates[0]); ++cand) {
     const int ept = candidates[cand >> 1];
     const int occ = 2 + (cand & 1);
-    if (precision != TP_PREC_FP32_MIXED && occ != 2) continue;
     c->ept = ept;
-    c->occupancy = occ;
+    c->occupancy[pi] = occ;
     int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);  // warm-up
     if (st) {
       c->ept = saved;
-      c->occupancy = saved_occ;
+      c->occupancy[pi] = saved_occ;
       return st;
     }
     cudaEventRecord(a, c->stream);
@@ -909,7 +909,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
     if (st) {
       c->ept = saved;
-      c->occupancy = saved_occ;
+      c->occupancy[pi] = saved_occ;
       return st;
     }
     float ms = 0.f;
@@ -922,9 +922,19 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   }
   c->ev_used = 0;
   c->ept = best;
-  c->occupancy = best_occ;
+  c->occupancy[pi] = best_occ;
   if (best_ept) *best_ept = best;
   if (best_events_per_s) *best_events_per_s = 2.0 * n * kBatch / (best_t * 1e-3);
+  return TP_OK;
+}
+
+int tp_set_occupancy(tp_ctx* c, int precision, int min_ctas_per_sm) {
+  if (!c) return TP_ERR_INVALID;
+  if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
+    return c->fail(TP_ERR_INVALID, "unknown precision");
+  if (min_ctas_per_sm != 2 && min_ctas_per_sm != 3)
+    return c->fail(TP_ERR_INVALID, "min_ctas_per_sm must be 2 or 3");
+  c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0] = min_ctas_per_sm;
   return TP_OK;
 }
 
@@ -994,7 +1004,8 @@ int tp_probe_fp64(tp_ctx* c, double out[5]) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, a, b);
       if (ms > 20.f || rep == 7) {
-        per_op_s[op] = (ms * 1e-3) / (threads * 8.0 * iters);  // seconds per operation
+        const double chains = op == 0 ? 16.0 : 8.0;  // independent chains per thread (k_probe)
+        per_op_s[op] = (ms * 1e-3) / (threads * chains * iters);  // seconds per operation
         break;
       }
       const double grow = ms > 0.01f ? 25.0 / ms : 64.0;

@@ -61,7 +61,7 @@ struct KParams {
   uint64_t n_batches;
   uint64_t num_events;   // events of the whole run
   int ept;               // xoshiro: events per thread
-  int occupancy;         // FP32 xoshiro kernel: minimum CTAs per SM (2 or 3)
+  int occupancy;         // xoshiro event kernels: minimum CTAs per SM (2 or 3)
   int precision;
   const void* batch_state;     // xoshiro: 4 x u64 per batch; ranf: 56 x i32
   const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
