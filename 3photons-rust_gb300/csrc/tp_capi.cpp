@@ -892,9 +892,11 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   const int saved = c->ept, saved_occ = c->occupancy[pi];
   double best_t = 1e300;
   int best = saved, best_occ = saved_occ;
-  for (int cand = 0; cand < 2 * (int)(sizeof candidates / sizeof candidates[0]); ++cand) {
-    const int ept = candidates[cand >> 1];
-    const int occ = 2 + (cand & 1);
+  // occupancy variants: FP64 2 or 3 CTAs per SM, FP32-mixed 2, 3 or 4
+  const int n_occ = precision == TP_PREC_FP32_MIXED ? 3 : 2;
+  for (int cand = 0; cand < n_occ * (int)(sizeof candidates / sizeof candidates[0]); ++cand) {
+    const int ept = candidates[cand / n_occ];
+    const int occ = 2 + cand % n_occ;
     c->ept = ept;
     c->occupancy[pi] = occ;
     int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);  // warm-up
@@ -903,17 +905,23 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
       c->occupancy[pi] = saved_occ;
       return st;
     }
-    cudaEventRecord(a, c->stream);
-    for (int rep = 0; rep < 2 && !st; ++rep) st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);
-    cudaEventRecord(b, c->stream);
-    if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
+    // the fastest of three separately timed runs (a sample takes about a
+    // millisecond, so single timings are noisy)
+    float ms = 1e30f;
+    for (int rep = 0; rep < 3 && !st; ++rep) {
+      cudaEventRecord(a, c->stream);
+      st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);
+      cudaEventRecord(b, c->stream);
+      if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
+      float one = 0.f;
+      if (!st) cudaEventElapsedTime(&one, a, b);
+      if (one < ms) ms = one;
+    }
     if (st) {
       c->ept = saved;
       c->occupancy[pi] = saved_occ;
       return st;
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
     if (ms < best_t) {
       best_t = ms;
       best = ept;
@@ -924,7 +932,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   c->ept = best;
   c->occupancy[pi] = best_occ;
   if (best_ept) *best_ept = best;
-  if (best_events_per_s) *best_events_per_s = 2.0 * n * kBatch / (best_t * 1e-3);
+  if (best_events_per_s) *best_events_per_s = (double)n * kBatch / (best_t * 1e-3);
   return TP_OK;
 }
 
@@ -932,8 +940,9 @@ int tp_set_occupancy(tp_ctx* c, int precision, int min_ctas_per_sm) {
   if (!c) return TP_ERR_INVALID;
   if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
     return c->fail(TP_ERR_INVALID, "unknown precision");
-  if (min_ctas_per_sm != 2 && min_ctas_per_sm != 3)
-    return c->fail(TP_ERR_INVALID, "min_ctas_per_sm must be 2 or 3");
+  const int hi = precision == TP_PREC_FP32_MIXED ? 4 : 3;
+  if (min_ctas_per_sm < 2 || min_ctas_per_sm > hi)
+    return c->fail(TP_ERR_INVALID, "min_ctas_per_sm: 2 or 3 (FP64), 2 to 4 (FP32-mixed)");
   c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0] = min_ctas_per_sm;
   return TP_OK;
 }

@@ -169,7 +169,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     cfg = workload_config(tp, ev32 * world)
     # events per thread and kernel variant from the autotuner (first 2048
     # batches of this workload)
-    tuned_ept = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 2048)[0] if not args.only else None
+    tuned_ept = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 16384)[0] if not args.only else None
     first32 = rank * nb
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)
     f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
@@ -411,7 +411,7 @@ def main():
             print(json.dumps(out))
         return
     costs = ctx.probe_fp64()
-    tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 2048)
+    tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 4096)
 
     dev = torch.device("cuda", local)
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)

@@ -210,8 +210,9 @@ int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
 
 /* Tuning: the xoshiro event kernel variant of `precision`, compiled for 2
- * (default) or 3 resident CTAs of 256 threads per SM (fewer registers per
- * thread, more warps to hide latency). Results are the same either way. */
+ * (default), 3 or (FP32-mixed only) 4 resident CTAs of 256 threads per SM
+ * (fewer registers per thread, more warps to hide latency). Results are the
+ * same either way. */
 int tp_set_occupancy(tp_ctx *ctx, int precision, int min_ctas_per_sm);
 
 /* ---- batched form: many parameter points --------------------------------
@@ -232,9 +233,10 @@ int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
 /* Autotuner: times the xoshiro event kernel of `precision` on the first
  * `sample_batches` batches of cfg for each candidate events-per-thread
  * (which fixes the block shape, ceil(10000 / ept) threads rounded to
- * warps) and each kernel variant of 2 or 3 resident CTAs per SM; keeps the
- * fastest for this context (all later launches, including tp_run_points;
- * the variant for `precision` only) and reports its events per thread. */
+ * warps) and each kernel variant (2 or 3 resident CTAs per SM, and 4 for
+ * FP32-mixed); keeps the fastest for this context (all later launches,
+ * including tp_run_points; the variant for `precision` only) and reports
+ * its events per thread. */
 int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,
                 uint64_t sample_batches, int *best_ept,
                 double *best_events_per_s);

@@ -132,7 +132,7 @@ def test_deterministic(ctx, cfg_valeurs):
     assert a.as_array().tobytes() == b.as_array().tobytes()
 
 
-@pytest.mark.parametrize("precision,occ", [(0, 2), (0, 3), (1, 2), (1, 3)])
+@pytest.mark.parametrize("precision,occ", [(0, 2), (0, 3), (1, 2), (1, 3), (1, 4)])
 def test_kernel_variants(tp, oracle, cfg_valeurs, precision, occ):
     """Both register/occupancy variants of the xoshiro event kernels."""
     cfg = cfg_valeurs.replace(num_events=60_001)
