@@ -251,6 +251,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
   kp.thread_poly = c->d_thread_poly;
+  kp.ranf_table = c->d_ranf_tab;
   if (extra) {
     kp.nx = extra->nx;
     kp.ny = extra->ny;

@@ -65,6 +65,7 @@ struct KParams {
   int precision;
   const void* batch_state;     // xoshiro: 4 x u64 per batch; ranf: 56 x i32
   const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
+  const uint32_t* ranf_table;  // ranf: x^(55 2^k) mod P, 55 coefficients per k
   BatchOut out;
   unsigned int* err;     // device error word (0 = fine)
   unsigned long long* recheck_count;  // FP32-mixed: events decided by the FP64 recheck
