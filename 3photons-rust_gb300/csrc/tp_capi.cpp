@@ -35,6 +35,7 @@ struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
   std::vector<uint64_t> xo_fe_chunk;                  // 64 x 4: x^(kFeChunk 2^k)
   std::vector<uint64_t> xo_fe_lane;                   // 32 x 4: x^(kFeLaneSpan l)
+  std::vector<uint64_t> xo_thread40;                  // 256 x 4: x^(12 kDefaultEpt j)
   std::vector<uint32_t> ranf;                         // 64 x 55
 };
 
@@ -69,6 +70,13 @@ const Tables& host_tables() {
       for (int w = 0; w < 4; ++w) t.xo_fe_lane[4 * l + w] = cur.w[w];
       cur = gf2_mulmod(cur, lane_step);
     }
+    t.xo_thread40.resize(4 * kTpb);
+    const Gf2Poly thread_step = gf2_xpow((uint64_t)kDrawsPerEvent * kDefaultEpt);
+    Gf2Poly tc{{1, 0, 0, 0}};
+    for (int j = 0; j < kTpb; ++j) {
+      for (int w = 0; w < 4; ++w) t.xo_thread40[4 * j + w] = tc.w[w];
+      tc = gf2_mulmod(tc, thread_step);
+    }
     t.ranf.resize(64 * 55);
     RanfPoly r = ranf_xpow(55);
     for (int k = 0; k < 64; ++k) {
@@ -92,6 +100,7 @@ struct tp_ctx {
   uint64_t* d_xo_draw = nullptr;
   uint32_t* d_ranf_tab = nullptr;
   uint64_t* d_thread_poly = nullptr;
+  uint64_t* d_thread_poly_binned = nullptr;  // x^(12 kDefaultEpt j): the binned pass's fixed shape
   int thread_poly_ept = 0;
   int32_t* d_ranf_window = nullptr;
   int64_t ranf_window_seed = -1;
@@ -243,14 +252,19 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   kp.precision = precision;
   kp.err = c->d_err;
   kp.recheck_count = c->d_recheck;
-  kp.ept = c->ept;
+  // the binned forward pass keeps 256 threads x 40 events per CTA whatever
+  // the tuned shape: its per-CTA shared histogram (up to 96 KB) limits how
+  // many CTAs fit on an SM, so small CTAs would leave SMs idle
+  const int ept = pass == Pass::kBinned ? kDefaultEpt : c->ept;
+  kp.ept = ept;
   kp.occupancy = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
   if (kind == TP_RNG_XOSHIRO256P) {
-    if (int st = ensure_thread_poly(c, c->ept)) return st;
+    if (pass != Pass::kBinned)
+      if (int st = ensure_thread_poly(c, c->ept)) return st;
   } else if (!jpb) {
     if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
-  kp.thread_poly = c->d_thread_poly;
+  kp.thread_poly = pass == Pass::kBinned ? c->d_thread_poly_binned : c->d_thread_poly;
   kp.ranf_table = c->d_ranf_tab;
   if (extra) {
     kp.nx = extra->nx;
@@ -295,7 +309,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     kp.out.sigma = out.sigma + c0;
     kp.out.variance = out.variance + c0;
     // xoshiro: enough warps for ceil(10000 / ept) threads; ranf: rounds of 256
-    const int need = (kBatch + c->ept - 1) / c->ept;
+    const int need = (kBatch + ept - 1) / ept;
     const int tpb = kind == TP_RNG_XOSHIRO256P ? ((need + 31) / 32) * 32 : kTpb;
     if (c->prof && (e0 = c->next_event()) && (e1 = c->next_event())) cudaEventRecord(e0, stream);
     if (pass == Pass::kBatches)
@@ -573,6 +587,7 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
   alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
   alloc((void**)&c->d_thread_poly, kTpb * 32, "tables");
+  alloc((void**)&c->d_thread_poly_binned, kTpb * 32, "tables");
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
@@ -592,6 +607,9 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st)
     st = c->cuda(cudaMemcpy(c->d_xo_fe_chunk, t.xo_fe_chunk.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_fe_lane, t.xo_fe_lane.data(), 128 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st)
+    st = c->cuda(cudaMemcpy(c->d_thread_poly_binned, t.xo_thread40.data(), kTpb * 32, cudaMemcpyHostToDevice),
+                 "tables");
   if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
   if (!st) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof(unsigned long long)), "recheck counter");
   if (st) {
@@ -608,7 +626,7 @@ void tp_destroy(tp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly,
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly, c->d_thread_poly_binned,
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate};

@@ -182,3 +182,19 @@ def test_invalid_arguments(tp, ctx, cfg_valeurs):
         ctx.set_events_per_thread(39)  # 257 threads: beyond one CTA
     # the context stays usable after errors
     ctx.run_batches(cfg_valeurs.replace(num_events=1000), 0, 1, rng="xoshiro")
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ranf_reseed_outside_canonical_range(tp, oracle, ctx, cfg_valeurs, precision):
+    """Batch 0's reseed 1000000970 leaves its state outside [0, 1e9)
+    (tp_ranf_state_at refuses it): that batch's warps reach their events by
+    stepping, the others by jump-ahead."""
+    cfg = cfg_valeurs.replace(num_events=40_000)
+    seed = 1000000970
+    gpu = ctx.run_batches(cfg, 0, 4, rng="ranf", seed=seed, jump_per_batch=True, precision=precision)
+    ref = oracle.run_batches(cfg, 0, 4, tp.rng_flags("ranf", True), seed)
+    if precision == tp.TP_PREC_FP64:
+        assert_batches_close(gpu, ref)
+    else:
+        assert np.array_equal(gpu.selected, ref.selected)
+        assert rel(gpu.sigma, ref.sigma) < 1e-6
