@@ -592,6 +592,100 @@ void skip_batch(Rng& rng, int flags, uint64_t n) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Positioning a stream far ahead by powers of its transition matrix, so that
+// batches deep inside a 1e9- or 1e10-event run can be checked without
+// stepping every draw before them. (The product jumps with characteristic
+// polynomials; this is an independent method.)
+// ---------------------------------------------------------------------------
+// xoshiro256+: the state after d steps is M^d s, M the GF(2) step matrix.
+void xoshiro_advance(Xoshiro& x, uint64_t d) {
+  static const Gf2Mat* step = [] {
+    Gf2Mat* m = new Gf2Mat;
+    for (int j = 0; j < 256; ++j) {
+      Xoshiro e;
+      for (int w = 0; w < 4; ++w) e.s[w] = 0;
+      e.s[j >> 6] = 1ull << (j & 63);
+      e.next_u64();
+      for (int w = 0; w < 4; ++w) m->col[j][w] = e.s[w];
+    }
+    return m;
+  }();
+  Gf2Mat* a = new Gf2Mat(*step);
+  Gf2Mat* b = new Gf2Mat;
+  while (d) {
+    if (d & 1) {
+      uint64_t out[4];
+      a->apply(x.s, out);
+      for (int w = 0; w < 4; ++w) x.s[w] = out[w];
+    }
+    d >>= 1;
+    if (d) {  // a <- a * a
+      for (int j = 0; j < 256; ++j) a->apply(a->col[j], b->col[j]);
+      std::swap(a, b);
+    }
+  }
+  delete a;
+  delete b;
+}
+
+// ranf: one reset maps the 55 slots linearly over Z/1e9 (for states in
+// [0, 1e9), where `v < 0 ? v + 1e9 : v` is v mod 1e9): block r = T^r block 0.
+struct RanfMat {
+  uint64_t m[55][55];  // m[i][j]: slot i + 1 from slot j + 1
+};
+
+void ranf_mat_mul(const RanfMat& A, const RanfMat& B, RanfMat& C) {
+  for (int i = 0; i < 55; ++i)
+    for (int j = 0; j < 55; ++j) {
+      uint64_t acc = 0;
+      for (int k = 0; k < 55; ++k) {
+        acc += A.m[i][k] * B.m[k][j];
+        if ((k & 15) == 15) acc %= (uint64_t)kModulo;
+      }
+      C.m[i][j] = acc % (uint64_t)kModulo;
+    }
+}
+
+bool ranf_advance(Ranf& r, uint64_t d) {
+  for (int s = 1; s < 56; ++s)
+    if (r.n[s] < 0 || r.n[s] >= kModulo) return false;
+  const uint64_t total = (uint64_t)(55 - r.index) + d;  // draws from the start of the current block
+  uint64_t blocks = total / 55;
+  RanfMat* a = new RanfMat;
+  for (int j = 0; j < 55; ++j) {  // column j: one reset of the unit vector e_j
+    int64_t v[56] = {0};
+    v[j + 1] = 1;
+    for (int i = 1; i < 25; ++i) v[i] = ((v[i] - v[i + 31]) % kModulo + kModulo) % kModulo;
+    for (int i = 25; i < 56; ++i) v[i] = ((v[i] - v[i - 24]) % kModulo + kModulo) % kModulo;
+    for (int i = 0; i < 55; ++i) a->m[i][j] = (uint64_t)v[i + 1];
+  }
+  RanfMat* t = new RanfMat;
+  while (blocks) {
+    if (blocks & 1) {
+      uint64_t out[55];
+      for (int i = 0; i < 55; ++i) {
+        uint64_t acc = 0;
+        for (int k = 0; k < 55; ++k) {
+          acc += a->m[i][k] * (uint64_t)r.n[k + 1];
+          if ((k & 15) == 15) acc %= (uint64_t)kModulo;
+        }
+        out[i] = acc % (uint64_t)kModulo;
+      }
+      for (int i = 0; i < 55; ++i) r.n[i + 1] = (int32_t)out[i];
+    }
+    blocks >>= 1;
+    if (blocks) {
+      ranf_mat_mul(*a, *a, *t);
+      std::swap(a, t);
+    }
+  }
+  delete a;
+  delete t;
+  r.index = (int)(55 - total % 55);
+  return true;
+}
+
 uint64_t batch_size(const tp_config& cfg, uint64_t b) {
   const uint64_t lo = b * kBatch;
   if (lo >= cfg.num_events) return 0;
@@ -859,8 +953,20 @@ int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
   const Consts k = make_consts(*cfg);
   Rng rng;
   rng.init(kind, seed);
-  // position the stream at first_batch
-  for (uint64_t b = 0; b < first_batch; ++b) {
+  // position the stream at first_batch: one-stream default-mode runs by a
+  // matrix power (12 draws per event), the others batch by batch
+  uint64_t skipped = 0;
+  if (!(flags & (TP_MODE_JUMP_PER_BATCH | TPO_MODE_FASTER_EVGEN)) && first_batch > 0) {
+    const uint64_t events = first_batch * (uint64_t)kBatch < cfg->num_events ? first_batch * (uint64_t)kBatch
+                                                                               : cfg->num_events;
+    if (kind == TP_RNG_XOSHIRO256P) {
+      xoshiro_advance(rng.xo, 12 * events);
+      skipped = first_batch;
+    } else if (ranf_advance(rng.ranf, 12 * events)) {
+      skipped = first_batch;
+    }
+  }
+  for (uint64_t b = skipped; b < first_batch; ++b) {
     if (flags & TP_MODE_JUMP_PER_BATCH)
       rng.jump();
     else
