@@ -167,8 +167,9 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     ev32 = 10 * events
     nb = (ev32 + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
     cfg = workload_config(tp, ev32 * world)
-    # events per thread and kernel variant from the autotuner (first 2048
-    # batches of this workload)
+    # events per thread and kernel variant from the autotuner (first 16384
+    # batches of this workload); single-leg profiling runs take them from
+    # --ept / --occupancy instead
     tuned_ept = ctx.autotune(cfg, tp.TP_PREC_FP32_MIXED, 16384)[0] if not args.only else None
     first32 = rank * nb
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)
@@ -369,6 +370,8 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--events", type=int, default=WORKLOAD_EVENTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ept", type=int, default=None, help="with --only: events per thread")
+    ap.add_argument("--occupancy", type=int, default=None, help="with --only: kernel variant, CTAs per SM")
     ap.add_argument("--only", choices=["fp64", "fp32", "fe"], default=None,
                     help="time one leg only (no e2e, no CPU baseline): for profiler captures")
     args = ap.parse_args()
@@ -390,6 +393,11 @@ def main():
     torch.cuda.set_device(local)
     tp = graft.package()
     ctx = tp.Context(local)
+    if args.only and args.ept:
+        ctx.set_events_per_thread(args.ept)
+    if args.only and args.occupancy:
+        prec = tp.TP_PREC_FP64 if args.only == "fp64" else tp.TP_PREC_FP32_MIXED
+        ctx.set_occupancy(prec, args.occupancy)
     events = args.events
     # weak scaling: every rank integrates its own 1e9-event range of one
     # world * 1e9-event run
@@ -411,7 +419,10 @@ def main():
             print(json.dumps(out))
         return
     costs = ctx.probe_fp64()
-    tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 4096)
+    if args.only and args.ept:
+        tuned_ept64 = args.ept
+    else:
+        tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 4096)
 
     dev = torch.device("cuda", local)
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)

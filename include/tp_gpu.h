@@ -40,7 +40,7 @@ extern "C" {
 /* ---- status codes ------------------------------------------------------ */
 #define TP_OK 0
 #define TP_ERR_INVALID (-1)     /* bad argument or configuration            */
-#define TP_ERR_UNSUPPORTED (-2) /* valid request this build does not serve  */
+#define TP_ERR_UNSUPPORTED (-2) /* valid request the library does not serve */
 #define TP_ERR_CUDA (-3)        /* CUDA allocation / launch / copy failure  */
 #define TP_ERR_DEVICE (-4)      /* a kernel raised its device error flag    */
 #define TP_ERR_TIMEOUT (-5)     /* a bounded device wait gave up            */
