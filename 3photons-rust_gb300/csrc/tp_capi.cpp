@@ -99,6 +99,7 @@ struct tp_ctx {
   uint64_t* d_xo_jump = nullptr;
   uint64_t* d_xo_draw = nullptr;
   uint32_t* d_ranf_tab = nullptr;
+  uint32_t* d_ranf_blocks = nullptr;  // x^(55 D), D < kRanfBlocksInBatch (built on first ranf run)
   uint64_t* d_thread_poly = nullptr;
   uint64_t* d_thread_poly_binned = nullptr;  // x^(12 kDefaultEpt j): the binned pass's fixed shape
   int thread_poly_ept = 0;
@@ -189,6 +190,28 @@ int ensure_thread_poly(tp_ctx* c, int ept) {
   return st;
 }
 
+// x^(55 D) mod P for every jump a warp of a ranf event kernel may make
+// within a batch, so that each warp positions its stream with one product
+int ensure_ranf_blocks(tp_ctx* c) {
+  if (c->d_ranf_blocks) return TP_OK;
+  std::vector<uint32_t> h(55 * (size_t)kRanfBlocksInBatch);
+  const RanfPoly step = ranf_xpow(55);
+  RanfPoly cur = ranf_xpow(0);
+  for (int d = 0; d < kRanfBlocksInBatch; ++d) {
+    for (int i = 0; i < 55; ++i) h[55 * (size_t)d + i] = cur.c[i];
+    cur = ranf_mulmod(cur, step);
+  }
+  uint32_t* dev = nullptr;
+  int st = c->cuda(cudaMalloc(&dev, h.size() * 4), "ranf block table");
+  if (!st) st = c->cuda(cudaMemcpy(dev, h.data(), h.size() * 4, cudaMemcpyHostToDevice), "ranf block table");
+  if (st) {
+    if (dev) cudaFree(dev);
+    return st;
+  }
+  c->d_ranf_blocks = dev;
+  return TP_OK;
+}
+
 // blocks 0 and 1 of a ranf stream (110 values) for the one-stream mode
 int ensure_ranf_window(tp_ctx* c, int32_t seed) {
   if (c->ranf_window_seed == (int64_t)seed) return TP_OK;
@@ -261,11 +284,14 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   if (kind == TP_RNG_XOSHIRO256P) {
     if (pass != Pass::kBinned)
       if (int st = ensure_thread_poly(c, c->ept)) return st;
-  } else if (!jpb) {
-    if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
+  } else {
+    if (int st = ensure_ranf_blocks(c)) return st;
+    if (!jpb)
+      if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
   kp.thread_poly = pass == Pass::kBinned ? c->d_thread_poly_binned : c->d_thread_poly;
   kp.ranf_table = c->d_ranf_tab;
+  kp.ranf_blocks = c->d_ranf_blocks;
   if (extra) {
     kp.nx = extra->nx;
     kp.ny = extra->ny;
@@ -626,7 +652,8 @@ void tp_destroy(tp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_thread_poly, c->d_thread_poly_binned,
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly,
+                  c->d_thread_poly_binned,
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate};

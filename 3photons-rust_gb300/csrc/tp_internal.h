@@ -15,6 +15,9 @@ constexpr double kMinPositive = 2.2250738585072014e-308;  // f64::MIN_POSITIVE
 constexpr int kBatch = TP_BATCH_SIZE;
 constexpr int kDrawsPerEvent = 12;  // default evgen: 3 photons x 4 draws
 constexpr uint64_t kDrawsPerBatch = (uint64_t)kDrawsPerEvent * kBatch;
+// blocks of 55 draws a warp may have to jump within one batch:
+// (54 + 12e4) / 55 + 1
+constexpr int kRanfBlocksInBatch = (54 + (int)kDrawsPerBatch) / 55 + 1;
 
 // Per-run constants of the event path, computed once on the host.
 struct EvConst {
@@ -66,6 +69,7 @@ struct KParams {
   const void* batch_state;     // xoshiro: 4 x u64 per batch; ranf: 56 x i32
   const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
   const uint32_t* ranf_table;  // ranf: x^(55 2^k) mod P, 55 coefficients per k
+  const uint32_t* ranf_blocks; // ranf: x^(55 D) mod P for D < kRanfBlocksInBatch
   BatchOut out;
   unsigned int* err;     // device error word (0 = fine)
   unsigned long long* recheck_count;  // FP32-mixed: events decided by the FP64 recheck
