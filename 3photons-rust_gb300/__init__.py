@@ -244,9 +244,13 @@ class Configuration:
         return (self.c.num_events + TP_BATCH_SIZE - 1) // TP_BATCH_SIZE
 
     def replace(self, **kw):
+        """A copy with some valeurs fields changed (names as in tp_config)."""
         c = CConfig()
         ctypes.pointer(c)[0] = self.c
+        fields = {f[0] for f in CConfig._fields_}
         for k, v in kw.items():
+            if k not in fields:
+                raise AttributeError("tp_config has no field %r" % k)
             setattr(c, k, v)
         return Configuration(c)
 
