@@ -247,3 +247,19 @@ def test_random_configurations(tp, oracle, ctx, cfg_sqrts1000):
         gpu32 = ctx.run_batches(cfg, 0, nb, rng=kind, precision=tp.TP_PREC_FP32_MIXED)
         assert np.array_equal(gpu32.selected, ref.selected)
         assert rel(gpu32.sigma, ref.sigma) < 1e-6
+
+
+@pytest.mark.parametrize("n", [1, 7, 10_001, 20_003])
+@pytest.mark.parametrize("rng", ["ranf", "xoshiro"])
+def test_tiny_and_ragged_runs(tp, oracle, ctx, cfg_valeurs, n, rng):
+    """Runs of 1 and 7 events, and last batches of 1 and 3 events: most
+    threads (and ranf warps) of those CTAs have no event."""
+    cfg = cfg_valeurs.replace(num_events=n)
+    nb = cfg.num_batches
+    ref = oracle.run_batches(cfg, 0, nb, tp.rng_flags(rng), tp.default_seed(rng))
+    assert_batches_close(ctx.run_batches(cfg, 0, nb, rng=rng), ref)
+    gpu32 = ctx.run_batches(cfg, 0, nb, rng=rng, precision=tp.TP_PREC_FP32_MIXED)
+    assert np.array_equal(gpu32.selected, ref.selected)
+    fe = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True)
+    fe_ref = oracle.run_batches(cfg, 0, nb, tp.rng_flags(rng, faster_evgen=True), tp.default_seed(rng))
+    assert_batches_close(fe, fe_ref)
