@@ -167,6 +167,7 @@ def library():
         "tp_profile": (i32, [vp, i32]),
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
+        "tp_probe_fp32": (i32, [vp, P(ctypes.c_double)]),
         "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
         "tp_run_batches_noalloc": (i32, [P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
         "tp_run_points": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_uint64), i32, i32,
@@ -413,6 +414,12 @@ class Context:
         out = (ctypes.c_double * 5)()
         self.check(library().tp_probe_fp64(self.h, out))
         return {"dfma_flops": out[0], "log": out[1], "sincos": out[2], "sqrt": out[3], "div": out[4]}
+
+    def probe_fp32(self):
+        """{'ffma_flops': FP32 flop/s, 'sfu_ops': special-function operations/s}."""
+        out = (ctypes.c_double * 2)()
+        self.check(library().tp_probe_fp32(self.h, out))
+        return {"ffma_flops": out[0], "sfu_ops": out[1]}
 
     def recheck_count(self, reset=True):
         """Events the FP32-mixed path settled with its FP64 recheck."""

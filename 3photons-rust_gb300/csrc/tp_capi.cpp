@@ -1036,6 +1036,52 @@ int tp_profile_read(tp_ctx* c, double* event_ms, uint64_t* event_launches, doubl
   return TP_OK;
 }
 
+namespace {
+// seconds per operation of k_probe's op `op` (chains per thread: 16 for the
+// FMA ops 0 and 5, else 8), timed until a launch lasts 20 ms
+int probe_op_seconds(tp_ctx* c, int op, double* seconds) {
+  int sms = 0;
+  if (int st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "probe")) return st;
+  double* sink = nullptr;
+  if (int st = c->cuda(cudaMalloc(&sink, sizeof(double)), "probe")) return st;
+  cudaEvent_t a = c->next_event(), b = c->next_event();
+  const int blocks = sms * 8, tpb = 256;
+  const double threads = (double)blocks * tpb;
+  const double chains = (op == 0 || op == 5) ? 16.0 : 8.0;
+  int st = TP_OK;
+  int iters = 16;
+  for (int rep = 0; rep < 8; ++rep) {
+    cudaEventRecord(a, c->stream);
+    st = launch_probe(op, iters, blocks, tpb, sink, c->stream);
+    cudaEventRecord(b, c->stream);
+    if (!st) st = c->cuda(cudaEventSynchronize(b), "probe");
+    if (st) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms > 20.f || rep == 7) {
+      *seconds = (ms * 1e-3) / (threads * chains * iters);
+      break;
+    }
+    const double grow = ms > 0.01f ? 25.0 / ms : 64.0;
+    iters = (int)(iters * (grow > 64.0 ? 64.0 : grow)) + 1;
+  }
+  cudaFree(sink);
+  c->ev_used = 0;
+  return st;
+}
+}  // namespace
+
+int tp_probe_fp32(tp_ctx* c, double out[2]) {
+  if (!c || !out) return TP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  double ffma = 0.0, mufu = 0.0;
+  if (int st = probe_op_seconds(c, 5, &ffma)) return st;
+  if (int st = probe_op_seconds(c, 6, &mufu)) return st;
+  out[0] = 2.0 / ffma;  // FP32 flop/s, an FMA counting 2
+  out[1] = 1.0 / mufu;  // special-function operations/s (log2, each with one add)
+  return TP_OK;
+}
+
 int tp_probe_fp64(tp_ctx* c, double out[5]) {
   if (!c || !out) return TP_ERR_INVALID;
   cudaSetDevice(c->device);

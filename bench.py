@@ -209,6 +209,20 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
         out["ratio_vs_fp64"] = value / fp64_value
     else:
         del out["ratio_vs_fp64"]
+    # roofline: t_min per event = max(W / P_fp32, N_sfu / P_sfu), with the
+    # canonical FP work W and special-function count N of an event and the
+    # FFMA and MUFU rates measured in this run (tp_probe_fp32)
+    rates = ctx.probe_fp32()
+    f_acc = float(sel.sum().item()) / ev32
+    w = 177.0 + 623.0 * f_acc
+    n_sfu = 9.0 + (5.0 + 3.0 * f_acc) + (2.0 + 9.0 * f_acc)
+    kernel_rate = ev32 * args.steps / (ev_ms * 1e-3)
+    t_fp, t_sfu = w / rates["ffma_flops"], n_sfu / rates["sfu_ops"]
+    out["roofline"] = {"bound": "fp32" if t_fp >= t_sfu else "sfu", "achieved": w * kernel_rate / 1e12,
+                       "peak": rates["ffma_flops"] / 1e12, "unit": "TFLOP/s", "frac": max(t_fp, t_sfu) * kernel_rate,
+                       "sfu_frac": t_sfu * kernel_rate, "flops_per_event": w, "sfu_ops_per_event": n_sfu,
+                       "peak_source": "FFMA and MUFU rates measured in this run (tp_probe_fp32)",
+                       "note": "the bit-exact xoshiro256+ stream (integer work) is outside W"}
     if world == 1 and acc64 is not None:
         acc32 = ctx.run_batches(cfg64, first, nb64, rng="xoshiro", seed=SEED, precision=tp.TP_PREC_FP32_MIXED)
         r32 = tp.merge_finalize(cfg64, acc32)

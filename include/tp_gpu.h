@@ -293,6 +293,10 @@ int tp_profile(tp_ctx *ctx, int enable);
 int tp_profile_read(tp_ctx *ctx, double *event_ms, uint64_t *event_launches,
                     double *seed_ms, uint64_t *seed_launches);
 int tp_probe_fp64(tp_ctx *ctx, double out[5]);
+/* tp_probe_fp32 measures this device's FP32 rates: out[0] = FFMA throughput
+ * in flop/s (an FMA counts 2), out[1] = special-function (MUFU log2)
+ * operations per second. */
+int tp_probe_fp32(tp_ctx *ctx, double out[2]);
 
 /* Number of events the FP32-mixed path handed to its FP64 recheck (events
  * whose cut decision lay within the FP32 error bound) since the context was
