@@ -99,6 +99,7 @@ struct PointsParams {
   uint64_t n_units;
   int ept;
   int precision;
+  int occupancy;  // FP32-mixed: kernel variant, minimum CTAs per SM (2 or 3)
 };
 
 // faster-evgen (src/evgen.rs:143-173, 221-249): an event takes 15 draws plus
@@ -179,7 +180,7 @@ void set_thread_error(const char* msg);
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
 int launch_binned(const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);
-int points_grid(int precision, int tpb);  // persistent grid size on the current device
+int points_grid(int precision, int occupancy, int tpb);  // persistent grid size on the current device
 int launch_adjoint(const KParams& p, int tpb, void* stream);
 // faster-evgen passes: chunk start states, chunk maps, thread start states,
 // events (batch_state = the thread start states)

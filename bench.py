@@ -316,7 +316,7 @@ def points_leg(tp, ctx, args):
     base = workload_config(tp, 1)
     cfgs, starts = tp.scan_points(base, 256, 12345)
     total = sum(c.num_events for c in cfgs)
-    ept, tuned_rate = ctx.autotune(base.replace(num_events=20_480_000), prec, 2048)
+    ept, tuned_rate = ctx.autotune(base.replace(num_events=163_840_000), prec, 16384)
     ctx.run_points(cfgs, starts, prec)  # captures the graph
     ctx.recheck_count(reset=True)
     ctx.profile(True)
