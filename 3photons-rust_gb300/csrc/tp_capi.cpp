@@ -126,6 +126,8 @@ struct tp_ctx {
   size_t fe_map_bytes = 0;
   void* d_fe_tstate = nullptr;
   size_t fe_tstate_bytes = 0;
+  void* d_fe_store = nullptr;  // one-stream runs: accept bits and lane states per chunk
+  size_t fe_store_bytes = 0;
   int sms = 0;
   // batched form (tp_run_points): device buffers and the captured graph
   struct Points {
@@ -376,6 +378,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
 constexpr uint64_t kFeMapLaunch = 16384;  // chunks per map launch
+constexpr uint64_t kFeStoreCap = 8ull << 30;  // bytes of device memory for the bit store
 // batches per starts + events launch: bounds the thread start states to
 // 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
 constexpr uint64_t kFePieceXo = 16384, kFePieceRanf = 4096;
@@ -501,6 +504,18 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     // batches past the run are empty: their event kernel CTAs store zeros
     const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
+    // the map pass keeps every chunk's accept bits (and xoshiro lane states)
+    // for the starts pass when they fit in kFeStoreCap (5.2 GB per 1e9 events)
+    const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
+    const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t);
+    if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
+      if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
+        return st;
+      fp.bits_store = static_cast<uint32_t*>(c->d_fe_store);
+      fp.lane_store = reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
+                                                  chunks * kFeStoreWords * sizeof(uint32_t));
+      fp.store_chunks = chunks;
+    }
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }
   const uint64_t piece = kind == TP_RNG_RANF ? kFePieceRanf : kFePieceXo;
@@ -656,7 +671,7 @@ void tp_destroy(tp_ctx* c) {
                   c->d_thread_poly_binned,
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
-                  c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate};
+                  c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);

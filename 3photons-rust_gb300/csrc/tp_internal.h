@@ -152,7 +152,15 @@ struct FeParams {
   int ept, tpb;
   void* thread_state;
   unsigned int* err;
+  // one-stream runs: the map pass keeps each chunk's accept bits
+  // (kFeStoreWords words) and, for xoshiro, its lanes' span-start states
+  // (32 x 4 words) for the starts pass; chunks >= store_chunks (or a null
+  // store) regenerate them
+  uint32_t* bits_store;
+  uint64_t* lane_store;
+  uint64_t store_chunks;
 };
+constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32);
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
