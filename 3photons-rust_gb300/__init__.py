@@ -169,6 +169,8 @@ def library():
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
         "tp_probe_fp32": (i32, [vp, P(ctypes.c_double)]),
         "tp_recheck_count": (i32, [vp, P(ctypes.c_uint64), i32]),
+        "tp_fp32_error": (i32, [vp, P(CConfig), i32, u64, u64, u64, P(ctypes.c_double), P(CBatchSoa),
+                                P(CBatchSoa)]),
         "tp_run_batches_noalloc": (i32, [P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
         "tp_run_points": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_uint64), i32, i32,
                                 P(ctypes.c_uint64), P(CBatchSoa), u64]),
@@ -420,6 +422,19 @@ class Context:
         out = (ctypes.c_double * 2)()
         self.check(library().tp_probe_fp32(self.h, out))
         return {"ffma_flops": out[0], "sfu_ops": out[1]}
+
+    def fp32_error(self, cfg, first_batch, n_batches, rng="ranf", seed=None, jump_per_batch=False, sorting=True):
+        """Per-batch relative error of the FP32-mixed sums against FP64 on the
+        same events (-1 where the selected counts differ), and both runs'
+        accumulators: (err[n], fp32, fp64)."""
+        seed = default_seed(rng) if seed is None else seed
+        err = np.zeros(n_batches, np.float64)
+        a32, a64 = BatchAccumulators(n_batches), BatchAccumulators(n_batches)
+        s32, s64 = a32.soa(), a64.soa()
+        self.check(library().tp_fp32_error(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch, sorting), seed,
+                                           first_batch, n_batches, err.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           ctypes.byref(s32), ctypes.byref(s64)))
+        return err, a32, a64
 
     def recheck_count(self, reset=True):
         """Events the FP32-mixed path settled with its FP64 recheck."""

@@ -2,6 +2,7 @@
 // device buffers, jump-ahead tables, batching of launches, error reporting.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1006,6 +1007,52 @@ int tp_set_occupancy(tp_ctx* c, int precision, int min_ctas_per_sm) {
   if (min_ctas_per_sm < 2 || min_ctas_per_sm > hi)
     return c->fail(TP_ERR_INVALID, "min_ctas_per_sm: 2 or 3 (FP64), 2 to 4 (FP32-mixed)");
   c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0] = min_ctas_per_sm;
+  return TP_OK;
+}
+
+int tp_fp32_error(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch,
+                  uint64_t n_batches, double* err_vs_fp64, tp_batch_soa* fp32, tp_batch_soa* fp64) {
+  if (!c) return TP_ERR_INVALID;
+  if (!err_vs_fp64) return c->fail(TP_ERR_INVALID, "null output array");
+  if (rng_kind & TP_MODE_FASTER_EVGEN) return c->fail(TP_ERR_UNSUPPORTED, "TP_MODE_FASTER_EVGEN runs in FP64 only");
+  if (n_batches == 0) return TP_OK;
+  if (n_batches > (1ull << 32)) return c->fail(TP_ERR_INVALID, "batch range too large");
+  const size_t n = n_batches;
+  std::vector<uint64_t> sel[2] = {std::vector<uint64_t>(n), std::vector<uint64_t>(n)};
+  std::vector<double> f[2] = {std::vector<double>(12 * n), std::vector<double>(12 * n)};
+  tp_batch_soa soa[2];
+  for (int k = 0; k < 2; ++k) {
+    soa[k] = tp_batch_soa{sel[k].data(), f[k].data(), f[k].data() + 5 * n, f[k].data() + 10 * n,
+                          f[k].data() + 11 * n};
+    const int precision = k == 0 ? TP_PREC_FP32_MIXED : TP_PREC_FP64;
+    if (int st = tp_run_batches(c, cfg, rng_kind, seed, first_batch, n_batches, precision, &soa[k])) return st;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    if (sel[0][i] != sel[1][i]) {
+      err_vs_fp64[i] = -1.0;
+      continue;
+    }
+    double e = 0.0;
+    const double scale_a = std::fabs(f[1][i]);  // spm2[0]: the A sum
+    for (int q = 0; q < 12; ++q) {
+      const double a = f[0][q * n + i], b = f[1][q * n + i];
+      // the mixed terms (spm2[3], spm2[4]) cancel: their natural scale is A's
+      const double scale = (q == 3 || q == 4) ? std::fmax(std::fabs(b), scale_a) : std::fabs(b);
+      if (scale > 0.0) e = std::fmax(e, std::fabs(a - b) / scale);
+      else if (a != 0.0) e = std::fmax(e, 1.0);
+    }
+    err_vs_fp64[i] = e;
+  }
+  tp_batch_soa* outs[2] = {fp32, fp64};
+  for (int k = 0; k < 2; ++k) {
+    tp_batch_soa* o = outs[k];
+    if (!o) continue;
+    if (o->selected) std::memcpy(o->selected, sel[k].data(), n * 8);
+    if (o->spm2) std::memcpy(o->spm2, soa[k].spm2, 5 * n * 8);
+    if (o->vars) std::memcpy(o->vars, soa[k].vars, 5 * n * 8);
+    if (o->sigma) std::memcpy(o->sigma, soa[k].sigma, n * 8);
+    if (o->variance) std::memcpy(o->variance, soa[k].variance, n * 8);
+  }
   return TP_OK;
 }
 

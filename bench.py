@@ -130,8 +130,15 @@ def cpu_baseline(tp, events_budget_s=3.0):
     oracle.run_batches(cfg, 0, nb, kind, SEED, threads)
     dt = time.perf_counter() - t0
     ev = nb * tp.TP_BATCH_SIZE
+    # one core as well: the reference's default, sequential scheduler
+    nb1 = 4
+    t0 = time.perf_counter()
+    oracle.run_batches(cfg, 0, nb1, kind, SEED, 1)
+    dt1 = time.perf_counter() - t0
     return {"value": ev / dt, "unit": "events/s", "cores": threads, "kind": "port",
-            "sample": "first %d batches (%d events) of the workload, FP64, %d threads" % (nb, ev, threads)}
+            "value_1core": nb1 * tp.TP_BATCH_SIZE / dt1,
+            "sample": "first %d batches (%d events) of the workload, FP64, %d threads; one core: first %d batches"
+                      % (nb, ev, threads, nb1)}
 
 
 RES_FIELDS = ("sigma", "prec", "beta_min", "ss_p", "inc_ss_p", "ss_m", "inc_ss_m")

@@ -304,6 +304,18 @@ int tp_probe_fp32(tp_ctx *ctx, double out[2]);
  * The reference has no mixed-precision path. */
 int tp_recheck_count(tp_ctx *ctx, uint64_t *count, int reset);
 
+/* The precision form's error, batch by batch: runs batches [first_batch,
+ * first_batch + n_batches) of the stream in FP32-mixed and in FP64 (the same
+ * events) and writes err_vs_fp64[i] = the largest relative difference of
+ * batch i's sums (spm2[5], vars[5], sigma, variance; the mixed terms on the
+ * scale of the A sum), or -1 where the selected counts differ. Either run's
+ * sums may be returned through the optional fp32 / fp64 arrays (NULL to
+ * skip). No counterpart in the reference, which has no mixed-precision path;
+ * TP_MODE_FASTER_EVGEN is FP64 only and gives TP_ERR_UNSUPPORTED. */
+int tp_fp32_error(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
+                  uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+                  double *err_vs_fp64, tp_batch_soa *fp32, tp_batch_soa *fp64);
+
 /* ---- host-side jump-ahead (no GPU) ----------------------------------------
  * State of a stream after `draws` draws, computed by polynomial jump-ahead:
  * checkpoint/resume and sharding need no stepping. xoshiro: seed_from_u64

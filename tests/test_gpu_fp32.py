@@ -8,6 +8,8 @@ quantities must agree with the FP64 path within 1e-6 relative. The
 interference (mixed) terms are compared on the larger of their own size and
 their natural scale sqrt(|A| |B+|): they are statistically zero at
 sqrt(s) = M_Z."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -54,3 +56,23 @@ def test_fp32_res_data_within_1e6(tp, ctx, request, cfg_name):
             else:
                 scale = max(abs(b), np.sqrt(abs(r64.spm2[s, 0] * r64.spm2[s, 1])))
                 assert abs(a - b) <= 1e-6 * scale, (s, c, a, b)
+
+
+def test_fp32_error_entry_point(tp, ctx, cfg_sqrts1000):
+    """tp_fp32_error: the precision form's per-batch error against FP64 on
+    the same events, for both streams."""
+    cfg = cfg_sqrts1000.replace(num_events=300_000)
+    for rng in ("xoshiro", "ranf"):
+        err, a32, a64 = ctx.fp32_error(cfg, 0, cfg.num_batches, rng=rng)
+        assert np.array_equal(a32.selected, a64.selected)
+        # a batch's sums are dominated by a few heavy events, whose FP32
+        # error reaches 1e-5; over the run the errors average out
+        assert (err >= 0).all() and err.max() < 1e-4
+        r32, r64 = tp.merge_finalize(cfg, a32), tp.merge_finalize(cfg, a64)
+        assert abs(r32.sigma - r64.sigma) <= 1e-6 * abs(r64.sigma)
+        ref64 = ctx.run_batches(cfg, 0, cfg.num_batches, rng=rng)
+        assert a64.as_array().tobytes() == ref64.as_array().tobytes()
+    err = np.zeros(1)
+    st = tp.library().tp_fp32_error(ctx.h, ctypes.byref(cfg.c), tp.rng_flags("xoshiro", faster_evgen=True), 1, 0, 1,
+                                    err.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None, None)
+    assert st == tp.TP_ERR_UNSUPPORTED
