@@ -688,19 +688,24 @@ def run_simulation_sharded(cfg, rank, world_size, run_batches, all_gather, **kw)
     return merge_finalize(cfg, BatchAccumulators.concatenate(parts))
 
 
-def run_simulation_resumable(cfg, checkpoint, run_batches, chunk_batches=1000):
+def run_simulation_resumable(cfg, checkpoint, run_batches, chunk_batches=1000, run_key=""):
     """Checkpointed run: integrates the batches chunk by chunk and, after
     every chunk, saves the per-batch sums so far to `checkpoint` (an .npz
     path, written atomically). A restarted call resumes at the first missing
     batch: batch b's stream is a pure function of (stream, seed, b), so the
     resumed run equals an uninterrupted one bit for bit.
     run_batches(first_batch, n) -> BatchAccumulators (e.g. a bound
-    Context.run_batches)."""
+    Context.run_batches). A checkpoint is only resumed by the same
+    configuration (every valeurs field) and the same `run_key`, a string the
+    caller makes from what run_batches binds (stream, seed, modes,
+    precision)."""
     nb = cfg.num_batches
     done = BatchAccumulators(0)
+    config_bytes = np.frombuffer(bytes(cfg.c), np.uint8)
     if os.path.exists(checkpoint):
         with np.load(checkpoint) as z:
-            if int(z["num_events"]) != cfg.num_events:
+            if (int(z["num_events"]) != cfg.num_events or "config" not in z
+                    or not np.array_equal(z["config"], config_bytes) or str(z["run_key"]) != run_key):
                 raise ValueError("checkpoint belongs to another run")
             done = BatchAccumulators.from_array(z["sums"])
     parts = [done]
@@ -712,7 +717,7 @@ def run_simulation_resumable(cfg, checkpoint, run_batches, chunk_batches=1000):
         acc = BatchAccumulators.concatenate(parts)
         parts = [acc]
         tmp = checkpoint + ".tmp.npz"
-        np.savez(tmp, sums=acc.as_array(), num_events=cfg.num_events)
+        np.savez(tmp, sums=acc.as_array(), num_events=cfg.num_events, config=config_bytes, run_key=run_key)
         os.replace(tmp, checkpoint)
     return merge_finalize(cfg, BatchAccumulators.concatenate(parts))
 

@@ -39,3 +39,18 @@ def test_checkpoint_of_another_run_is_refused(tp, oracle, cfg_valeurs, tmp_path)
     tp.run_simulation_resumable(cfg, ckpt, run, chunk_batches=1)
     with pytest.raises(ValueError):
         tp.run_simulation_resumable(cfg.replace(num_events=30_000), ckpt, run)
+
+
+def test_checkpoint_keyed_on_configuration_and_run(tp, oracle, cfg_valeurs, tmp_path):
+    """Same event count, other physics or other stream: refused."""
+    ckpt = str(tmp_path / "run.npz")
+    cfg = cfg_valeurs.replace(num_events=20_000)
+    run = lambda f, n: oracle.run_batches(cfg, f, n, 0, tp.RANF_DEFAULT_SEED, threads=1)
+    tp.run_simulation_resumable(cfg, ckpt, run, chunk_batches=1, run_key="ranf 234612947")
+    with pytest.raises(ValueError):
+        tp.run_simulation_resumable(cfg.replace(beta_plus=0.5), ckpt, run, run_key="ranf 234612947")
+    with pytest.raises(ValueError):
+        tp.run_simulation_resumable(cfg, ckpt, run, run_key="ranf 1")
+    # the same run resumes (nothing left to do)
+    res = tp.run_simulation_resumable(cfg, ckpt, run, run_key="ranf 234612947")
+    assert res.selected_events > 0
