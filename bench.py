@@ -240,13 +240,14 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     return out
 
 
-def grad_leg(tp, ctx, args, events):
+def grad_leg(tp, ctx, args, events, fit_steps=200):
     """The differentiation form: a 20 x 20 binned Gaussian log-likelihood of
     a model run (beta+- = 0, M_Z = 91.187, Gamma_Z = 2.490, seed 12345)
     against pseudo-data (beta+ = 0.3, beta- = -0.2, seed 777), 1e9 events
     each, FP32-mixed. Times the forward pass (value) and the adjoint pass,
     i.e. d(lnL, sigma)/d(beta+, beta-, M_Z, Gamma_Z) by recomputing every
-    event from its stream position."""
+    event from its stream position, then recovers beta+- with `fit_steps`
+    gradient steps."""
     prec = tp.TP_PREC_FP32_MIXED
     nb = (events + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
     bins = tp.binning(20, 20)
@@ -271,10 +272,24 @@ def grad_leg(tp, ctx, args, events):
     ga, dsa = model.analytic_gradient(theta)
     grad = flux * g @ dk
     f, a = sum(fwd) / len(fwd), sum(adj) / len(adj)
-    return {"events": events, "precision": "fp32_mixed", "bins": "20x20", "forward_ms": 1e3 * f,
-            "adjoint_ms": 1e3 * a, "grad_over_fwd": a / f, "gradient_step_over_fwd": (f + a) / f,
-            "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": (flux * s @ dk).tolist(),
-            "max_rel_dev_vs_analytic": float(np.max(np.abs(grad - ga)) / np.max(np.abs(ga)))}
+    out = {"events": events, "precision": "fp32_mixed", "bins": "20x20", "forward_ms": 1e3 * f,
+           "adjoint_ms": 1e3 * a, "grad_over_fwd": a / f, "gradient_step_over_fwd": (f + a) / f,
+           "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": (flux * s @ dk).tolist(),
+           "max_rel_dev_vs_analytic": float(np.max(np.abs(grad - ga)) / np.max(np.abs(ga)))}
+    if fit_steps:
+        # recover beta+- from the pseudo-data: natural-gradient steps, each a
+        # forward and an adjoint pass over all events. Only beta-^2 enters the
+        # weights, so the start is off beta- = 0 (where d/dbeta- vanishes) and
+        # beta- is recovered up to its sign.
+        t0 = time.perf_counter()
+        theta_fit, cov = tp.fit(model, (0.1, -0.1, 91.187, 2.49), steps=fit_steps)
+        wall = time.perf_counter() - t0
+        err = np.sqrt(np.diag(cov))
+        truth = np.array([0.3, -0.2])
+        out["fit"] = {"steps": fit_steps, "start": [0.1, -0.1], "truth": truth.tolist(),
+                      "beta": theta_fit[:2].tolist(), "beta_err": err.tolist(),
+                      "pull": ((theta_fit[:2] - truth) / err).tolist(), "ms_per_step": 1e3 * wall / fit_steps}
+    return out
 
 
 def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=None):
