@@ -81,7 +81,9 @@ extern "C" {
  * stream's accept bits from draw 0, also for first_batch > 0), then runs the
  * events. FP64 only (TP_PREC_FP32_MIXED gives TP_ERR_UNSUPPORTED), batch
  * accumulators only (tp_run_batches / tp_run_batches_async); the _async call
- * waits for the boundary pass before it queues the event kernels. */
+ * waits for the boundary pass before it queues the event kernels. A
+ * one-stream run keeps the pass's accept bits in device memory (about 5.8 GB
+ * per 1e9 events, not above 8 GiB; longer runs recompute them). */
 #define TP_RNG_RANF 0
 #define TP_RNG_XOSHIRO256P 1
 #define TP_RNG_KIND_MASK 0xff
