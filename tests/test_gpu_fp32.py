@@ -76,3 +76,37 @@ def test_fp32_error_entry_point(tp, ctx, cfg_sqrts1000):
     st = tp.library().tp_fp32_error(ctx.h, ctypes.byref(cfg.c), tp.rng_flags("xoshiro", faster_evgen=True), 1, 0, 1,
                                     err.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None, None)
     assert st == tp.TP_ERR_UNSUPPORTED
+
+
+def _headline_results(text):
+    """sigma, its standard deviation and relative precision, beta_min and the
+    B+- significances with their uncertainties: the res.data lines after the
+    configuration echo (src/output.rs:62-142)."""
+    import re
+    out = []
+    for line in text.splitlines()[17:26]:
+        if ":" in line:
+            out.extend(float(t) for t in re.findall(r"[-+]?\d+\.?\d*(?:[eE][-+]?\d+)?", line.split(":")[-1]))
+    return np.array(out)
+
+
+def test_fp32_mixed_against_the_reference_f32_build(tp, ctx, cfg_valeurs):
+    """The reference's own all-FP32 build (`--features f32`) selects 1428
+    events more than its FP64 build on the N = 1e7 standard-random golden run,
+    and its res.data numbers move accordingly. The FP32-mixed path selects
+    exactly the FP64 events and stays far closer to the FP64 golden on every
+    number."""
+    from conftest import golden
+
+    res = tp.run_simulation(cfg_valeurs, rng="xoshiro", precision=tp.TP_PREC_FP32_MIXED, ctx=ctx)
+    g64 = golden("res.data", "standard-random")
+    g32 = golden("res.data", "standard-random,f32")
+    assert res.res_data().splitlines()[1] == g64.splitlines()[1]
+    assert g32.splitlines()[1] != g64.splitlines()[1]
+    ours, ref64, ref32 = _headline_results(res.res_data()), _headline_results(g64), _headline_results(g32)
+    assert ours.shape == ref64.shape == ref32.shape == (8,)
+    err_ours = np.abs(ours - ref64) / np.abs(ref64)
+    err_f32 = np.abs(ref32 - ref64) / np.abs(ref64)  # includes its 5-digit printing
+    assert err_ours.max() < 1e-5
+    # the f32 build's largest deviation (1.6e-3) is far above ours
+    assert err_f32.max() > 100 * err_ours.max()
