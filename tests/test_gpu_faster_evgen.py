@@ -107,3 +107,16 @@ def test_unsupported_combinations(tp, ctx, cfg_valeurs):
     assert st == tp.TP_ERR_UNSUPPORTED
     # the context stays usable
     ctx.run_batches(cfg, 0, 1, rng="xoshiro", faster_evgen=True)
+
+
+@pytest.mark.parametrize("seed", [42049, 176937])
+def test_chunk_entered_past_the_mapped_offsets(tp, oracle, ctx, cfg_valeurs, seed):
+    """Chunk maps cover entry offsets 0..31. These xoshiro seeds (found by
+    simulating the stream on the CPU) have an event of more than 32 draws
+    straddling a chunk boundary, so chunk 2 (seed 42049, entry 32) or chunk 3
+    (seed 176937, entry 34) is entered past the mapped offsets and mapped
+    again for its actual entry."""
+    cfg = cfg_valeurs.replace(num_events=30_000)
+    nb = cfg.num_batches
+    gpu = ctx.run_batches(cfg, 0, nb, rng="xoshiro", seed=seed, faster_evgen=True)
+    assert_batches_close(gpu, oracle_batches(tp, oracle, cfg, 0, nb, "xoshiro", False, True, seed))
