@@ -66,3 +66,16 @@ def test_full_run_fp32_selects_the_fp64_events(tp, full_run):
     a = tp.merge_finalize(cfg, whole)
     b = tp.merge_finalize(cfg, fp32)
     assert abs(b.sigma - a.sigma) <= 1e-6 * abs(a.sigma)
+
+
+@pytest.mark.parametrize("rng", ["xoshiro", "ranf"])
+def test_batches_2_to_the_40_in(tp, oracle, ctx, cfg_sqrts1000, rng):
+    """Batches around index 2^40 of a 2^40 + 8 batch run (1.3e17 draws in):
+    64-bit draw offsets far past the benchmark sizes, against the oracle's
+    transition-matrix powers; FP32-mixed selects the same events."""
+    first = 2**40 - 2
+    cfg = cfg_sqrts1000.replace(num_events=(2**40 + 8) * tp.TP_BATCH_SIZE)
+    ref = oracle.run_batches(cfg, first, 4, tp.rng_flags(rng), tp.default_seed(rng))
+    assert_batches_close(ctx.run_batches(cfg, first, 4, rng=rng), ref)
+    gpu32 = ctx.run_batches(cfg, first, 4, rng=rng, precision=tp.TP_PREC_FP32_MIXED)
+    assert np.array_equal(gpu32.selected, ref.selected)
