@@ -6,6 +6,8 @@ bit-exact. Floating-point sums: per batch within 1e-12 relative (the GPU
 sums a batch in a tree, the reference left to right; measured differences
 are ~1e-15). Momenta: within 64 ulps (CUDA's log/sin/cos and glibc's may
 differ in their last bit)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -180,6 +182,19 @@ def test_invalid_arguments(tp, ctx, cfg_valeurs):
         ctx.set_events_per_thread(0)
     with pytest.raises(tp.TPError) as e:
         ctx.set_events_per_thread(39)  # 257 threads: beyond one CTA
+    # batch ranges past the ABI's 2^46 limit, unknown precision and mode flags
+    with pytest.raises(tp.TPError) as e:
+        ctx.run_batches(cfg_valeurs, 2**46 + 1, 1, rng="xoshiro")
+    assert e.value.code == tp.TP_ERR_INVALID
+    with pytest.raises(tp.TPError) as e:
+        ctx.run_batches(cfg_valeurs, 0, 1, rng="xoshiro", precision=7)
+    assert e.value.code == tp.TP_ERR_INVALID
+    acc = tp.BatchAccumulators(1)
+    st = tp.library().tp_run_batches(ctx.h, ctypes.byref(cfg_valeurs.c), tp.TP_RNG_XOSHIRO256P | 0x800, 1, 0, 1,
+                                     tp.TP_PREC_FP64, ctypes.byref(acc.soa()))
+    assert st == tp.TP_ERR_INVALID
+    # empty ranges are no-ops
+    assert ctx.run_batches(cfg_valeurs, 0, 0, rng="xoshiro").n == 0
     # the context stays usable after errors
     ctx.run_batches(cfg_valeurs.replace(num_events=1000), 0, 1, rng="xoshiro")
 
