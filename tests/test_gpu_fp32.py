@@ -38,16 +38,22 @@ def test_fp32_decisions_match_fp64(tp, ctx, cfg_valeurs, rng, jump):
         assert np.max(np.abs(f32.spm2[c] - f64.spm2[c]) / scale) < 1e-5
 
 
+@pytest.mark.parametrize("rng", ["xoshiro", "ranf"])
 @pytest.mark.parametrize("cfg_name", ["cfg_valeurs", "cfg_sqrts1000"])
-def test_fp32_res_data_within_1e6(tp, ctx, request, cfg_name):
+def test_fp32_res_data_within_1e6(tp, ctx, request, cfg_name, rng):
+    """A systematic error in the FP32 draws adds up over the events instead
+    of averaging out (ranf's n * fl(1e-9) moved A by 1.1e-6). The
+    significances' uncertainties rest on the squared weights of a few heavy
+    events, whose FP32 errors (up to 1e-5 each) average out more slowly:
+    2e-6 at 1e7 events here, 1.4e-7 at 1e9."""
     cfg = request.getfixturevalue(cfg_name)
     cfg = cfg.replace(num_events=min(cfg.num_events, 10_000_000))
-    r32 = tp.run_simulation(cfg, rng="xoshiro", precision=tp.TP_PREC_FP32_MIXED, ctx=ctx)
-    r64 = tp.run_simulation(cfg, rng="xoshiro", ctx=ctx)
+    r32 = tp.run_simulation(cfg, rng=rng, precision=tp.TP_PREC_FP32_MIXED, ctx=ctx)
+    r64 = tp.run_simulation(cfg, rng=rng, ctx=ctx)
     assert r32.selected_events == r64.selected_events
     for f in ("sigma", "beta_min", "ss_p", "ss_m", "prec", "inc_ss_p", "inc_ss_m"):
         a, b = getattr(r32, f), getattr(r64, f)
-        assert abs(a - b) <= 1e-6 * abs(b), (f, a, b)
+        assert abs(a - b) <= (1e-5 if f.startswith("inc_") else 1e-6) * abs(b), (f, a, b)
     for s in range(2):
         for c in range(5):
             a, b = r32.spm2[s, c], r64.spm2[s, c]
