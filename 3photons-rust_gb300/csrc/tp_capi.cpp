@@ -942,9 +942,11 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   if (check_config(cfg)) return c->fail(TP_ERR_INVALID, "invalid configuration");
   if (sample_batches == 0 || sample_batches > kChunk) return c->fail(TP_ERR_INVALID, "sample_batches out of range");
   cudaSetDevice(c->device);
-  // events per thread -> threads per CTA = ceil(10000 / ept) rounded to warps
-  // (more events per thread: fewer per-thread stream jumps of 256 steps)
-  static const int candidates[] = {40, 50, 64, 80, 100, 125, 160, 200, 250};
+  // events per thread -> threads per CTA = ceil(10000 / ept) rounded to
+  // warps (more events per thread: fewer per-thread stream jumps of 256
+  // steps). The candidates fill their last warp: ceil(10000 / ept) is at
+  // or just below 256, 192, 160, 128, 96, 64 and 32 threads.
+  static const int candidates[] = {40, 53, 63, 79, 105, 157, 313};
   const size_t n = sample_batches;
   if (int st = ensure(c, &c->d_out, &c->out_bytes, n * 13 * 8, "output buffers")) return st;
   auto* sel = static_cast<uint64_t*>(c->d_out);
@@ -962,7 +964,12 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     const int occ = 2 + cand % n_occ;
     c->ept = ept;
     c->occupancy[pi] = occ;
-    int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);  // warm-up
+    // whole waves of resident CTAs, so that a candidate whose last wave
+    // the sample happens to leave nearly empty is not penalised for it
+    const int tpb = (((int)kBatch + ept - 1) / ept + 31) / 32 * 32;
+    const uint64_t wave = (uint64_t)events_wave(precision, occ, tpb);
+    const uint64_t ns = n >= wave ? n / wave * wave : n;
+    int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, ns, precision, o, c->stream);  // warm-up
     if (st) {
       c->ept = saved;
       c->occupancy[pi] = saved_occ;
@@ -973,7 +980,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     float ms = 1e30f;
     for (int rep = 0; rep < 3 && !st; ++rep) {
       cudaEventRecord(a, c->stream);
-      st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, n, precision, o, c->stream);
+      st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, ns, precision, o, c->stream);
       cudaEventRecord(b, c->stream);
       if (!st) st = c->cuda(cudaEventSynchronize(b), "autotune");
       float one = 0.f;
@@ -985,8 +992,9 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
       c->occupancy[pi] = saved_occ;
       return st;
     }
-    if (ms < best_t) {
-      best_t = ms;
+    const double t = ms / (double)ns;  // per batch
+    if (t < best_t) {
+      best_t = t;
       best = ept;
       best_occ = occ;
     }
@@ -995,7 +1003,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   c->ept = best;
   c->occupancy[pi] = best_occ;
   if (best_ept) *best_ept = best;
-  if (best_events_per_s) *best_events_per_s = (double)n * kBatch / (best_t * 1e-3);
+  if (best_events_per_s) *best_events_per_s = (double)kBatch / (best_t * 1e-3);
   return TP_OK;
 }
 

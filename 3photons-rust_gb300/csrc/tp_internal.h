@@ -189,6 +189,7 @@ int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* s
 int launch_binned(const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);
 int points_grid(int precision, int occupancy, int tpb);  // persistent grid size on the current device
+int events_wave(int precision, int occupancy, int tpb);  // resident xoshiro event CTAs on the current device
 int launch_adjoint(const KParams& p, int tpb, void* stream);
 // faster-evgen passes: chunk start states, chunk maps, thread start states,
 // events (batch_state = the thread start states)

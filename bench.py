@@ -458,7 +458,7 @@ def main():
     if args.only and args.ept:
         tuned_ept64 = args.ept
     else:
-        tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 4096)
+        tuned_ept64, _ = ctx.autotune(cfg, tp.TP_PREC_FP64, 8192)
 
     dev = torch.device("cuda", local)
     sel = torch.zeros(nb, dtype=torch.int64, device=dev)

@@ -236,7 +236,8 @@ int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
  * `sample_batches` batches of cfg for each candidate events-per-thread
  * (which fixes the block shape, ceil(10000 / ept) threads rounded to
  * warps) and each kernel variant (2 or 3 resident CTAs per SM, and 4 for
- * FP32-mixed); keeps the fastest for this context (all later launches,
+ * FP32-mixed), each on a whole number of waves of resident CTAs within
+ * the sample; keeps the fastest for this context (all later launches,
  * including tp_run_points; the variant for `precision` only) and reports
  * its events per thread. */
 int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,

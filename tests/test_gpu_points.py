@@ -52,7 +52,7 @@ def test_autotune_keeps_results(tp, cfg_sqrts1000):
     with tp.Context(0) as ctx:
         ref = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", precision=1)
         ept, rate = ctx.autotune(cfg, 1, 512)
-        assert ept in (40, 50, 64, 80, 100, 125, 160, 200, 250) and rate > 1e9
+        assert ept in (40, 53, 63, 79, 105, 157, 313) and rate > 1e9
         got = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", precision=1)
     # the block shape regroups the per-thread FP32 sums: same events, sums
     # equal to FP32 accumulation accuracy
