@@ -164,6 +164,7 @@ def library():
         "tp_dump_events_prec": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, vp]),
         "tp_set_events_per_thread": (i32, [vp, i32]),
         "tp_set_occupancy": (i32, [vp, i32, i32]),
+        "tp_get_tuning": (i32, [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "tp_profile": (i32, [vp, i32]),
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
         "tp_probe_fp64": (i32, [vp, P(ctypes.c_double)]),
@@ -400,6 +401,12 @@ class Context:
     def set_occupancy(self, precision, min_ctas_per_sm):
         """xoshiro event kernel variant of `precision`: 2 or 3 CTAs per SM."""
         self.check(library().tp_set_occupancy(self.h, precision, min_ctas_per_sm))
+
+    def tuning(self, precision):
+        """(events per thread, kernel variant) in use for `precision`."""
+        ept, occ = ctypes.c_int(), ctypes.c_int()
+        self.check(library().tp_get_tuning(self.h, precision, ctypes.byref(ept), ctypes.byref(occ)))
+        return ept.value, occ.value
 
     def profile(self, enable=True):
         self.check(library().tp_profile(self.h, 1 if enable else 0))

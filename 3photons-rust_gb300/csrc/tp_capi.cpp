@@ -1007,6 +1007,15 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   return TP_OK;
 }
 
+int tp_get_tuning(tp_ctx* c, int precision, int* ept, int* min_ctas_per_sm) {
+  if (!c) return TP_ERR_INVALID;
+  if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
+    return c->fail(TP_ERR_INVALID, "unknown precision");
+  if (ept) *ept = c->ept;
+  if (min_ctas_per_sm) *min_ctas_per_sm = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
+  return TP_OK;
+}
+
 int tp_set_occupancy(tp_ctx* c, int precision, int min_ctas_per_sm) {
   if (!c) return TP_ERR_INVALID;
   if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)

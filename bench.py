@@ -209,6 +209,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     value = world * ev32 * args.steps / (sum(step_ms) * 1e-3)
     out = {"value": value, "unit": "events/s", "events_per_step": ev32 * world, "ms_per_step": sum(step_ms) / len(step_ms),
            "autotuned_events_per_thread": tuned_ept,
+           "kernel_variant_ctas_per_sm": ctx.tuning(tp.TP_PREC_FP32_MIXED)[1],
            "kernel": "k_events_xoshiro_fp32", "kernel_ms": ev_ms / args.steps,
            "gpu_launches": int(ev_launches + seed_launches), "ratio_vs_fp64": None,
            "rechecked_fraction": rechecked / (ev32 * args.steps)}
@@ -353,6 +354,7 @@ def points_leg(tp, ctx, args):
             "value": total * args.steps / (graph_ms * 1e-3), "unit": "events/s",
             "graph_ms_per_step": graph_ms / args.steps, "graph_launches": int(launches),
             "e2e": total * args.steps / wall, "autotuned_events_per_thread": ept,
+            "kernel_variant_ctas_per_sm": ctx.tuning(prec)[1],
             "autotune_sample_events_per_s": tuned_rate,
             "min_max_events_per_point": [min(c.num_events for c in cfgs), max(c.num_events for c in cfgs)],
             "rechecked_fraction": ctx.recheck_count(reset=True) / (total * args.steps),
@@ -545,7 +547,8 @@ def main():
                                "1e9 events = 1e5 batches of 1e4 per GPU",
                    "events_per_step": events * world, "batches": nb * world, "precision": "fp64",
                    "l2": "flushed between steps (256 MiB write)", "parallelism": "batch-range shards, no collective",
-                   "autotuned_events_per_thread": tuned_ept64},
+                   "autotuned_events_per_thread": tuned_ept64,
+                   "kernel_variant_ctas_per_sm": ctx.tuning(tp.TP_PREC_FP64)[1]},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "DFMA throughput measured in this run (tp_probe_fp64)",

@@ -217,6 +217,10 @@ int tp_set_events_per_thread(tp_ctx *ctx, int ept);
  * same either way. */
 int tp_set_occupancy(tp_ctx *ctx, int precision, int min_ctas_per_sm);
 
+/* Tuning in use for `precision`: events per thread and kernel variant
+ * (minimum resident CTAs per SM), as set or picked by tp_autotune. */
+int tp_get_tuning(tp_ctx *ctx, int precision, int *ept, int *min_ctas_per_sm);
+
 /* ---- batched form: many parameter points --------------------------------
  * No counterpart in the reference, which runs one configuration per process.
  * Runs n_points complete runs, each with its own configuration (physics,
