@@ -646,20 +646,29 @@ def fisher_matrix(model, theta, hist=None):
     return J.T @ (J / model.var[:, None])
 
 
-def fit(model, theta0, steps=200, lr=0.5, free=(0, 1), damping=1e-3):
-    """Maximises ln L over the parameters `free` (indices into theta) with
-    `steps` natural-gradient steps: theta += lr (F + damping) ^-1 g, where g
-    comes from the forward + adjoint passes on the GPU and F is the
-    Gauss-Newton Fisher matrix of the same forward pass. Returns (theta,
-    covariance estimate F^-1 at the end)."""
+def fit(model, theta0, steps=200, lr=0.5, free=(0, 1), damping=1e-3, tol=0.0, info=None):
+    """Maximises ln L over the parameters `free` (indices into theta) with at
+    most `steps` natural-gradient steps: theta += lr (F + damping) ^-1 g,
+    where g comes from the forward + adjoint passes on the GPU and F is the
+    Gauss-Newton Fisher matrix of the same forward pass. Stops early once a
+    step moves every free parameter by less than `tol` of its standard error
+    sqrt(diag F^-1) (tol = 0: never). Returns (theta, covariance estimate
+    F^-1 at the end); `info`, a dict, receives the steps taken."""
     theta = np.array(theta0, np.float64)
     idx = list(free)
     F = None
+    taken = 0
     for _ in range(steps):
         _, g, _, _ = model.gradient(theta)
         F = fisher_matrix(model, theta)[np.ix_(idx, idx)]
         Fd = F + damping * np.trace(F) / len(idx) * np.eye(len(idx))
-        theta[idx] += lr * np.linalg.solve(Fd, g[idx])
+        step = lr * np.linalg.solve(Fd, g[idx])
+        theta[idx] += step
+        taken += 1
+        if tol > 0 and np.all(np.abs(step) < tol * np.sqrt(np.diag(np.linalg.inv(F)))):
+            break
+    if info is not None:
+        info["steps"] = taken
     return theta, np.linalg.inv(F)
 
 

@@ -36,7 +36,6 @@ struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
   std::vector<uint64_t> xo_fe_chunk;                  // 64 x 4: x^(kFeChunk 2^k)
   std::vector<uint64_t> xo_fe_lane;                   // 32 x 4: x^(kFeLaneSpan l)
-  std::vector<uint64_t> xo_thread40;                  // 256 x 4: x^(12 kDefaultEpt j)
   std::vector<uint32_t> ranf;                         // 64 x 55
 };
 
@@ -71,13 +70,6 @@ const Tables& host_tables() {
       for (int w = 0; w < 4; ++w) t.xo_fe_lane[4 * l + w] = cur.w[w];
       cur = gf2_mulmod(cur, lane_step);
     }
-    t.xo_thread40.resize(4 * kTpb);
-    const Gf2Poly thread_step = gf2_xpow((uint64_t)kDrawsPerEvent * kDefaultEpt);
-    Gf2Poly tc{{1, 0, 0, 0}};
-    for (int j = 0; j < kTpb; ++j) {
-      for (int w = 0; w < 4; ++w) t.xo_thread40[4 * j + w] = tc.w[w];
-      tc = gf2_mulmod(tc, thread_step);
-    }
     t.ranf.resize(64 * 55);
     RanfPoly r = ranf_xpow(55);
     for (int k = 0; k < 64; ++k) {
@@ -94,16 +86,17 @@ struct tp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  int ept = kDefaultEpt;
-  int occupancy[2] = {2, 2};  // xoshiro event kernel variant per precision: min CTAs per SM
+  // per precision (FP64, FP32-mixed): xoshiro events per thread and event
+  // kernel variant (min CTAs per SM)
+  int ept[2] = {kDefaultEpt, kDefaultEpt};
+  int occupancy[2] = {2, 2};
   uint64_t* d_xo_batch = nullptr;
   uint64_t* d_xo_jump = nullptr;
   uint64_t* d_xo_draw = nullptr;
   uint32_t* d_ranf_tab = nullptr;
   uint32_t* d_ranf_blocks = nullptr;  // x^(55 D), D < kRanfBlocksInBatch (built on first ranf run)
-  uint64_t* d_thread_poly = nullptr;
-  uint64_t* d_thread_poly_binned = nullptr;  // x^(12 kDefaultEpt j): the binned pass's fixed shape
-  int thread_poly_ept = 0;
+  uint64_t* d_thread_poly[2] = {nullptr, nullptr};  // per precision: x^(12 ept j), j < 256
+  int thread_poly_ept[2] = {0, 0};
   int32_t* d_ranf_window = nullptr;
   int64_t ranf_window_seed = -1;
   void* d_state = nullptr;
@@ -176,8 +169,11 @@ int ensure(tp_ctx* c, void** p, size_t* have, size_t need, const char* what) {
   return st;
 }
 
-int ensure_thread_poly(tp_ctx* c, int ept) {
-  if (c->thread_poly_ept == ept) return TP_OK;
+int prec_index(int precision) { return precision == TP_PREC_FP32_MIXED ? 1 : 0; }
+
+int ensure_thread_poly(tp_ctx* c, int pi) {
+  const int ept = c->ept[pi];
+  if (c->thread_poly_ept[pi] == ept) return TP_OK;
   std::vector<uint64_t> h(4 * kTpb);
   const Gf2Poly step = gf2_xpow((uint64_t)kDrawsPerEvent * ept);
   Gf2Poly cur{{1, 0, 0, 0}};
@@ -185,11 +181,11 @@ int ensure_thread_poly(tp_ctx* c, int ept) {
     for (int w = 0; w < 4; ++w) h[4 * j + w] = cur.w[w];
     cur = gf2_mulmod(cur, step);
   }
-  int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
+  int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[pi], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
                    "upload thread polynomials");
   if (st) return st;
   st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
-  if (st == TP_OK) c->thread_poly_ept = ept;
+  if (st == TP_OK) c->thread_poly_ept[pi] = ept;
   return st;
 }
 
@@ -278,21 +274,21 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   kp.precision = precision;
   kp.err = c->d_err;
   kp.recheck_count = c->d_recheck;
-  // the binned forward pass keeps 256 threads x 40 events per CTA whatever
-  // the tuned shape: its per-CTA shared histogram (up to 96 KB) limits how
-  // many CTAs fit on an SM, so small CTAs would leave SMs idle
-  const int ept = pass == Pass::kBinned ? kDefaultEpt : c->ept;
+  // the binned forward pass runs several batches per CTA at the tuned
+  // shape: its per-CTA shared histogram (up to 96 KB) limits how many CTAs
+  // fit on an SM
+  const int pi = prec_index(precision);
+  const int ept = c->ept[pi];
   kp.ept = ept;
-  kp.occupancy = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
+  kp.occupancy = c->occupancy[pi];
   if (kind == TP_RNG_XOSHIRO256P) {
-    if (pass != Pass::kBinned)
-      if (int st = ensure_thread_poly(c, c->ept)) return st;
+    if (int st = ensure_thread_poly(c, pi)) return st;
   } else {
     if (int st = ensure_ranf_blocks(c)) return st;
     if (!jpb)
       if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
-  kp.thread_poly = pass == Pass::kBinned ? c->d_thread_poly_binned : c->d_thread_poly;
+  kp.thread_poly = c->d_thread_poly[pi];
   kp.ranf_table = c->d_ranf_tab;
   kp.ranf_blocks = c->d_ranf_blocks;
   if (extra) {
@@ -302,6 +298,10 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     kp.x_inv_w = extra->x_inv_w;
     kp.y_lo = extra->y_lo;
     kp.y_inv_w = extra->y_inv_w;
+    kp.f_x_lo = extra->f_x_lo;
+    kp.f_x_inv_w = extra->f_x_inv_w;
+    kp.f_y_lo = extra->f_y_lo;
+    kp.f_y_inv_w = extra->f_y_inv_w;
     kp.bin_weight = c->d_binw;
     kp.hist = c->d_hist;
     kp.adj = c->d_adj;
@@ -475,8 +475,8 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
   fp.kind = kind;
   fp.jpb = jpb;
   fp.err = c->d_err;
-  fp.ept = c->ept;
-  const int tpb = (((kBatch + c->ept - 1) / c->ept) + 31) / 32 * 32;
+  fp.ept = c->ept[0];  // FP64 only
+  const int tpb = (((kBatch + fp.ept - 1) / fp.ept) + 31) / 32 * 32;
   fp.tpb = tpb;
   fp.num_events = n_total;
   if (kind == TP_RNG_XOSHIRO256P) {
@@ -496,7 +496,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
   kp.num_events = n_total;
   kp.precision = precision;
   kp.err = c->d_err;
-  kp.ept = c->ept;
+  kp.ept = fp.ept;
   const size_t state_bytes = kind == TP_RNG_RANF ? 56 * sizeof(int32_t) : 4 * sizeof(uint64_t);
   const uint64_t b_end = first_batch + n_batches;
   // one stream: compose once through the last event of the range
@@ -597,6 +597,10 @@ int binning_params(tp_ctx* c, const tp_config* cfg, const tp_binning* bins, KPar
   kp->x_inv_w = bins->n_emax / (xh - xl);
   kp->y_lo = yl;
   kp->y_inv_w = bins->n_cos / (yh - yl);
+  kp->f_x_lo = (float)kp->x_lo;
+  kp->f_x_inv_w = (float)kp->x_inv_w;
+  kp->f_y_lo = (float)kp->y_lo;
+  kp->f_y_inv_w = (float)kp->y_inv_w;
   return TP_OK;
 }
 
@@ -628,8 +632,8 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_xo_jump, 256 * 8, "tables");
   alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
   alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
-  alloc((void**)&c->d_thread_poly, kTpb * 32, "tables");
-  alloc((void**)&c->d_thread_poly_binned, kTpb * 32, "tables");
+  alloc((void**)&c->d_thread_poly[0], kTpb * 32, "tables");
+  alloc((void**)&c->d_thread_poly[1], kTpb * 32, "tables");
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
@@ -649,9 +653,6 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st)
     st = c->cuda(cudaMemcpy(c->d_xo_fe_chunk, t.xo_fe_chunk.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_fe_lane, t.xo_fe_lane.data(), 128 * 8, cudaMemcpyHostToDevice), "tables");
-  if (!st)
-    st = c->cuda(cudaMemcpy(c->d_thread_poly_binned, t.xo_thread40.data(), kTpb * 32, cudaMemcpyHostToDevice),
-                 "tables");
   if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
   if (!st) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof(unsigned long long)), "recheck counter");
   if (st) {
@@ -668,8 +669,7 @@ void tp_destroy(tp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly,
-                  c->d_thread_poly_binned,
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly[0], c->d_thread_poly[1],
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
@@ -765,7 +765,7 @@ int tp_dump_events_prec(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t 
 int tp_set_events_per_thread(tp_ctx* c, int ept) {
   if (!c) return TP_ERR_INVALID;
   if (ept <= 0 || (TP_BATCH_SIZE + ept - 1) / ept > kTpb) return c->fail(TP_ERR_INVALID, "events per thread out of range");
-  c->ept = ept;
+  c->ept[0] = c->ept[1] = ept;
   return TP_OK;
 }
 
@@ -844,7 +844,8 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   std::vector<uint32_t> unit_point(n_units);
   for (uint32_t p = 0; p < n_points; ++p)
     for (uint64_t u = unit0[p]; u < unit0[p + 1]; ++u) unit_point[u] = p;
-  if (int st = ensure_thread_poly(c, c->ept)) return st;
+  const int pi = prec_index(precision);
+  if (int st = ensure_thread_poly(c, pi)) return st;
   // one device buffer, 256-byte aligned sections
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_pts = 0, o_ev = o_pts + al(n_points * sizeof(EvConst)), o_u0 = o_ev + al(n_points * 8),
@@ -866,16 +867,16 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   pp.unit_point = reinterpret_cast<const uint32_t*>(base + o_up);
   pp.unit_state = reinterpret_cast<uint64_t*>(base + o_us);
   pp.batch_table = c->d_xo_batch;
-  pp.thread_poly = c->d_thread_poly;
+  pp.thread_poly = c->d_thread_poly[pi];
   pp.counter = reinterpret_cast<unsigned long long*>(base + o_cnt);
   pp.recheck_count = c->d_recheck;
   auto* sel = reinterpret_cast<uint64_t*>(base + o_out);
   auto* f = reinterpret_cast<double*>(sel + n_units);
   pp.out = BatchOut{sel, f, f + 5 * n_units, f + 10 * n_units, f + 11 * n_units, n_units};
   pp.n_units = n_units;
-  pp.ept = c->ept;
+  pp.ept = c->ept[pi];
   pp.precision = precision;
-  pp.occupancy = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
+  pp.occupancy = c->occupancy[pi];
   int st = TP_OK;
   auto up = [&](size_t off, const void* src, size_t n) {
     if (!st) st = c->cuda(cudaMemcpyAsync(base + off, src, n, cudaMemcpyHostToDevice, c->stream), "upload points");
@@ -887,14 +888,14 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   up(o_up, unit_point.data(), n_units * 4);
   if (st) return st;
   // the seeding + persistent launches are captured once per shape and replayed
-  const uint64_t key[7] = {n_points, n_units, (uint64_t)precision, (uint64_t)c->ept, (uint64_t)mode_flags,
+  const uint64_t key[7] = {n_points, n_units, (uint64_t)precision, (uint64_t)pp.ept, (uint64_t)mode_flags,
                            (uint64_t)(uintptr_t)c->pts.buf, (uint64_t)pp.occupancy};
   if (!c->pts.exec || std::memcmp(key, c->pts.key, sizeof key) != 0) {
     if (c->pts.exec) cudaGraphExecDestroy(c->pts.exec);
     if (c->pts.graph) cudaGraphDestroy(c->pts.graph);
     c->pts.exec = nullptr;
     c->pts.graph = nullptr;
-    const int need = (kBatch + c->ept - 1) / c->ept;
+    const int need = (kBatch + pp.ept - 1) / pp.ept;
     const int tpb = ((need + 31) / 32) * 32;
     st = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
     if (st) return st;
@@ -954,7 +955,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   BatchOut o{sel, f, f + 5 * n, f + 10 * n, f + 11 * n, n};
   cudaEvent_t a = c->next_event(), b = c->next_event();
   const int pi = precision == TP_PREC_FP32_MIXED ? 1 : 0;
-  const int saved = c->ept, saved_occ = c->occupancy[pi];
+  const int saved = c->ept[pi], saved_occ = c->occupancy[pi];
   double best_t = 1e300;
   int best = saved, best_occ = saved_occ;
   // occupancy variants: FP64 2 or 3 CTAs per SM, FP32-mixed 2, 3 or 4
@@ -962,7 +963,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
   for (int cand = 0; cand < n_occ * (int)(sizeof candidates / sizeof candidates[0]); ++cand) {
     const int ept = candidates[cand / n_occ];
     const int occ = 2 + cand % n_occ;
-    c->ept = ept;
+    c->ept[pi] = ept;
     c->occupancy[pi] = occ;
     // whole waves of resident CTAs, so that a candidate whose last wave
     // the sample happens to leave nearly empty is not penalised for it
@@ -971,7 +972,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     const uint64_t ns = n >= wave ? n / wave * wave : n;
     int st = run_async(c, cfg, TP_RNG_XOSHIRO256P, 12345, 0, ns, precision, o, c->stream);  // warm-up
     if (st) {
-      c->ept = saved;
+      c->ept[pi] = saved;
       c->occupancy[pi] = saved_occ;
       return st;
     }
@@ -988,7 +989,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
       if (one < ms) ms = one;
     }
     if (st) {
-      c->ept = saved;
+      c->ept[pi] = saved;
       c->occupancy[pi] = saved_occ;
       return st;
     }
@@ -1000,7 +1001,7 @@ int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_
     }
   }
   c->ev_used = 0;
-  c->ept = best;
+  c->ept[pi] = best;
   c->occupancy[pi] = best_occ;
   if (best_ept) *best_ept = best;
   if (best_events_per_s) *best_events_per_s = (double)kBatch / (best_t * 1e-3);
@@ -1011,7 +1012,7 @@ int tp_get_tuning(tp_ctx* c, int precision, int* ept, int* min_ctas_per_sm) {
   if (!c) return TP_ERR_INVALID;
   if (precision != TP_PREC_FP64 && precision != TP_PREC_FP32_MIXED)
     return c->fail(TP_ERR_INVALID, "unknown precision");
-  if (ept) *ept = c->ept;
+  if (ept) *ept = c->ept[prec_index(precision)];
   if (min_ctas_per_sm) *min_ctas_per_sm = c->occupancy[precision == TP_PREC_FP32_MIXED ? 1 : 0];
   return TP_OK;
 }

@@ -77,6 +77,7 @@ struct KParams {
   // its angle to the electron beam; bin = ix * ny + iy
   int nx, ny;
   double x_lo, x_inv_w, y_lo, y_inv_w;
+  float f_x_lo, f_x_inv_w, f_y_lo, f_y_inv_w;  // the same, for the FP32-mixed kernels
   const double* bin_weight;  // adjoint: d lnL / d mu_b per bin
   double* hist;              // binned forward: [nx * ny][8] accumulators
   double* adj;               // adjoint: [n_batches][10] per-batch sums

@@ -206,9 +206,9 @@ int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
                         uint64_t seed, uint64_t first_event, uint64_t n,
                         int precision, tp_event_dump *out);
 
-/* Tuning: events each thread integrates in the xoshiro kernels (default
- * 40; ceil(10000 / ept) must not exceed 256). No counterpart in the
- * reference, whose batches run on one CPU thread each. */
+/* Tuning: events each thread integrates in the xoshiro kernels, for both
+ * precisions (default 40; ceil(10000 / ept) must not exceed 256). No
+ * counterpart in the reference, whose batches run on one CPU thread each. */
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
 
 /* Tuning: the xoshiro event kernel variant of `precision`, compiled for 2
@@ -241,9 +241,9 @@ int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
  * (which fixes the block shape, ceil(10000 / ept) threads rounded to
  * warps) and each kernel variant (2 or 3 resident CTAs per SM, and 4 for
  * FP32-mixed), each on a whole number of waves of resident CTAs within
- * the sample; keeps the fastest for this context (all later launches,
- * including tp_run_points; the variant for `precision` only) and reports
- * its events per thread. */
+ * the sample; keeps the fastest pair for `precision` in this context (its
+ * later launches of that precision: batches, tp_run_points, the binned
+ * passes) and reports its events per thread. */
 int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,
                 uint64_t sample_batches, int *best_ept,
                 double *best_events_per_s);

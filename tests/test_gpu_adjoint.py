@@ -91,8 +91,9 @@ def test_torch_autograd_function(setup):
 
 
 def test_gradient_fit_recovers_betas(tp, ctx, cfg_sqrts1000):
-    # 200 natural-gradient steps (adjoint gradient, Gauss-Newton Fisher
-    # preconditioner) on (beta+, beta-) from near the model point beta+- = 0.
+    # natural-gradient steps (adjoint gradient, Gauss-Newton Fisher
+    # preconditioner) on (beta+, beta-) from near the model point beta+- = 0,
+    # until a step moves both by less than 1e-3 of their errors.
     # Only beta-^2 enters the weights, so the data fix |beta-|; beta+ also
     # enters linearly through the interference terms.
     prec = tp.TP_PREC_FP32_MIXED
@@ -102,7 +103,9 @@ def test_gradient_fit_recovers_betas(tp, ctx, cfg_sqrts1000):
     model_cfg = cfg_sqrts1000.replace(num_events=20_000_000, beta_plus=0.0, beta_minus=0.0)
     model = tp.BinnedGaussianLikelihood(ctx, model_cfg, SEED_MODEL, model_cfg.num_batches, data, data_cfg, bins,
                                         precision=prec)
-    theta, cov = tp.fit(model, [0.05, 0.05, 91.187, 2.49], steps=200, lr=0.5)
+    info = {}
+    theta, cov = tp.fit(model, [0.05, 0.05, 91.187, 2.49], steps=200, lr=0.5, tol=1e-3, info=info)
+    assert info["steps"] < 200
     err = np.sqrt(np.diag(cov))
     # statistical errors of data and model both enter (the likelihood only
     # counts the data's): allow 5 of the Fisher errors, at least 0.02
