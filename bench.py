@@ -281,16 +281,15 @@ def grad_leg(tp, ctx, args, events, fit_steps=200):
         # recover beta+- from the pseudo-data: natural-gradient steps, each a
         # forward and an adjoint pass over all events. Only beta-^2 enters the
         # weights, so the start is off beta- = 0 (where d/dbeta- vanishes) and
-        # beta- is recovered up to its sign. The fit stops once a step moves
-        # both by less than 1e-3 of their standard errors.
+        # beta- is recovered up to its sign. All fit_steps steps run (the
+        # workload's 200), although the fit converges in about 20.
         t0 = time.perf_counter()
         info = {}
-        theta_fit, cov = tp.fit(model, (0.1, -0.1, 91.187, 2.49), steps=fit_steps, tol=1e-3, info=info)
+        theta_fit, cov = tp.fit(model, (0.1, -0.1, 91.187, 2.49), steps=fit_steps, info=info)
         wall = time.perf_counter() - t0
         err = np.sqrt(np.diag(cov))
         truth = np.array([0.3, -0.2])
-        out["fit"] = {"steps": info["steps"], "max_steps": fit_steps, "tol_in_std_errors": 1e-3,
-                      "start": [0.1, -0.1], "truth": truth.tolist(),
+        out["fit"] = {"steps": info["steps"], "start": [0.1, -0.1], "truth": truth.tolist(),
                       "beta": theta_fit[:2].tolist(), "beta_err": err.tolist(),
                       "pull": ((theta_fit[:2] - truth) / err).tolist(), "ms_per_step": 1e3 * wall / info["steps"]}
     return out
