@@ -116,3 +116,27 @@ def test_fp32_mixed_against_the_reference_f32_build(tp, ctx, cfg_valeurs):
     assert err_ours.max() < 1e-5
     # the f32 build's largest deviation (1.6e-3) is far above ours
     assert err_f32.max() > 100 * err_ours.max()
+
+
+@pytest.mark.parametrize("rng", ["xoshiro", "ranf"])
+def test_fp32_event_dumps(tp, ctx, cfg_sqrts1000, rng):
+    """tp_dump_events_prec: the FP32-mixed path's view of single events
+    (photons in energy order, as the reference lays them out) against the
+    FP64 view of the same draws: the same cut verdicts, FP32-close momenta
+    and helicity sums, and the rechecked events flagged."""
+    n = 20_000
+    d64 = ctx.dump_events(cfg_sqrts1000, 0, n, rng=rng)
+    d32 = ctx.dump_events(cfg_sqrts1000, 0, n, rng=rng, precision=tp.TP_PREC_FP32_MIXED)
+    assert np.array_equal(d32["uniforms"], d64["uniforms"])
+    assert np.array_equal(d32["cut"], d64["cut"])
+    assert d32["reserved"].sum() < 1e-3 * n and set(np.unique(d32["reserved"])) <= {0, 1}
+    kept = d64["cut"] == 0
+    assert 0.5 * n < kept.sum() < n
+    # FP32 rounding of the raw momenta, amplified by the conformal map's
+    # cancellation R_E^2 / R^2 (hundreds for a few events)
+    dp = np.abs(d32["p_out"][kept] - d64["p_out"][kept]).max(axis=(1, 2)) / cfg_sqrts1000.e_total
+    assert dp.max() < 2e-4 and np.median(dp) < 2e-7, (dp.max(), np.median(dp))
+    for c in (0, 1, 2):
+        a, b = d32["m2_sums"][kept, c], d64["m2_sums"][kept, c]
+        rel = np.abs(a - b) / np.abs(b)
+        assert rel.max() < 1e-3 and np.median(rel) < 1e-6, (c, rel.max(), np.median(rel))
