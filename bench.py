@@ -167,6 +167,23 @@ def precision_report(r32, r64):
     return out, stat
 
 
+def issue_roofline(torch, dev, fp32, clocks):
+    """The FP32-mixed kernel is issue-bound (no pipe saturated): its second
+    roofline is warp instructions issued per second against the schedulers'
+    ceiling (4 per SM per clock at the SM clock sampled in this run). The
+    instructions per event of this build come from its ncu capture
+    (profiles/issue.json); the rate is this run's."""
+    path = os.path.join(ROOT, "profiles", "issue.json")
+    if not os.path.exists(path) or not clocks.get("sm_mhz") or "kernel_events_per_s" not in fp32:
+        return
+    prof = json.load(open(path))
+    peak = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * clocks["sm_mhz"] * 1e6
+    achieved = prof["warp_inst_per_event"] * fp32["kernel_events_per_s"]
+    fp32["roofline"]["issue"] = {"achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+                                 "frac": achieved / peak, "warp_inst_per_event": prof["warp_inst_per_event"],
+                                 "source": prof["source"]}
+
+
 def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value, acc64, cfg64, first, nb64):
     """The precision form: FP32 phase space, spinors and amplitudes, FP64 batch
     sums, FP64 recheck of events near a cut boundary, on 1e10 events per GPU
@@ -226,6 +243,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     n_sfu = 9.0 + (5.0 + 3.0 * f_acc) + (2.0 + 9.0 * f_acc)
     kernel_rate = ev32 * args.steps / (ev_ms * 1e-3)
     t_fp, t_sfu = w / rates["ffma_flops"], n_sfu / rates["sfu_ops"]
+    out["kernel_events_per_s"] = kernel_rate
     out["roofline"] = {"bound": "fp32" if t_fp >= t_sfu else "sfu", "achieved": w * kernel_rate / 1e12,
                        "peak": rates["ffma_flops"] / 1e12, "unit": "TFLOP/s", "frac": max(t_fp, t_sfu) * kernel_rate,
                        "sfu_frac": t_sfu * kernel_rate, "flops_per_event": w, "sfu_ops_per_event": n_sfu,
@@ -563,6 +581,7 @@ def main():
         "result": {"sigma_pb": sigma, "selected": selected},
         "fp32_mixed": fp32,
     }
+    issue_roofline(torch, dev, fp32, line["clocks"])
     if world == 1:
         line["grad"] = grad_leg(tp, ctx, args, events)
         line["batched"] = points_leg(tp, ctx, args)
