@@ -179,6 +179,8 @@ def library():
         "tp_binned_forward": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp]),
         "tp_binned_adjoint": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp,
                                     P(ctypes.c_double), P(ctypes.c_double)]),
+        "tp_grad": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp,
+                          P(ctypes.c_double), P(ctypes.c_double)]),
         "tp_coupling_factors": (i32, [P(CConfig), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
         "tp_xoshiro_state_at": (i32, [u64, u64, u64, P(ctypes.c_uint64)]),
         "tp_ranf_state_at": (i32, [ctypes.c_int32, u64, P(ctypes.c_int32), P(ctypes.c_int32)]),
@@ -525,6 +527,18 @@ class Context:
                                                seed, first_batch, n_batches, precision, ctypes.byref(binning),
                                                ctypes.c_void_p(w.ctypes.data), g, sm))
         return np.array(g[:]), np.array(sm[:])
+
+    def grad(self, cfg, first_batch, n_batches, binning, bin_weight, seed=XOSHIRO_DEFAULT_SEED,
+             precision=TP_PREC_FP64, jump_per_batch=False):
+        """tp_grad: (d lnL/dtheta, d sigma/dtheta) for theta = (beta+, beta-,
+        M_Z, Gamma_Z), r = bin_weight = d lnL / d mu per bin."""
+        w = np.ascontiguousarray(bin_weight, np.float64)
+        dl = (ctypes.c_double * 4)()
+        ds = (ctypes.c_double * 4)()
+        self.check(library().tp_grad(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch), seed,
+                                     first_batch, n_batches, precision, ctypes.byref(binning),
+                                     ctypes.c_void_p(w.ctypes.data), dl, ds))
+        return np.array(dl[:]), np.array(ds[:])
 
     def dump_events(self, cfg, first_event, n, rng="ranf", seed=None, jump_per_batch=False, sorting=True,
                     precision=TP_PREC_FP64):

@@ -817,6 +817,26 @@ int tp_binned_adjoint(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t se
   return TP_OK;
 }
 
+int tp_grad(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+            int precision, const tp_binning* bins, const double* bin_weight, double dlnl_dtheta[4],
+            double dsigma_dtheta[4]) {
+  if (!c) return TP_ERR_INVALID;
+  double g[5], sg[5], k[5], dk[20], flux = 0.0;
+  if (int st = tp_binned_adjoint(c, cfg, rng_kind, seed, first_batch, n_batches, precision, bins, bin_weight, g, sg))
+    return st;
+  if (int st = tp_coupling_factors(cfg, k, dk, &flux)) return c->fail(st, "coupling factors");
+  for (int i = 0; i < 4; ++i) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < 5; ++q) {
+      a += g[q] * dk[4 * q + i];
+      b += sg[q] * dk[4 * q + i];
+    }
+    if (dlnl_dtheta) dlnl_dtheta[i] = flux * a;
+    if (dsigma_dtheta) dsigma_dtheta[i] = flux * b;
+  }
+  return TP_OK;
+}
+
 int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uint64_t* starts, int mode_flags,
                   int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
   if (!c) return TP_ERR_INVALID;

@@ -281,6 +281,16 @@ int tp_binned_adjoint(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
                       int precision, const tp_binning *bins,
                       const double *bin_weight, double g[5], double s[5]);
 
+/* The gradient in one call: tp_binned_adjoint composed with
+ * tp_coupling_factors, d lnL/dtheta[i] = flux sum_c g_c dK_c/dtheta_i and
+ * d sigma/dtheta[i] = flux sum_c s_c dK_c/dtheta_i for theta = (beta+,
+ * beta-, M_Z, Gamma_Z) at the theta of cfg, r = bin_weight as in
+ * tp_binned_adjoint. Either output may be NULL. */
+int tp_grad(tp_ctx *ctx, const tp_config *cfg, int rng_kind, uint64_t seed,
+            uint64_t first_batch, uint64_t n_batches, int precision,
+            const tp_binning *bins, const double *bin_weight,
+            double dlnl_dtheta[4], double dsigma_dtheta[4]);
+
 /* K_c(theta) and dK_c/d(beta+, beta-, M_Z, Gamma_Z) (dk[4 c + i], forward-
  * mode dual numbers) at the theta of cfg, and the incident flux 1/(2 s)
  * (src/resacc.rs:178) that turns sums of w into cross sections (pb). */

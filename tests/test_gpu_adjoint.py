@@ -54,6 +54,19 @@ def test_adjoint_matches_analytic_gradient(setup, theta):
     assert np.allclose(dsigma, dsa, rtol=1e-10, atol=1e-10 * np.abs(dsa).max())
 
 
+def test_grad_entry_point(tp, setup):
+    """tp_grad composes the adjoint sums with dK/dtheta in one call."""
+    bins, _, _, _, model = setup
+    theta = (0.25, -0.1, 91.187, 2.49)
+    lnl, grad, sigma, dsigma = model.gradient(theta)
+    cfg = model.theta_cfg(theta)
+    _, _, mu = model.value(theta)
+    r = -(mu - model.data) / model.var
+    g, ds = model.ctx.grad(cfg, 0, model.n_batches, bins, r, model.seed, model.precision)
+    assert np.allclose(g, grad, rtol=1e-13, atol=1e-13 * np.abs(grad).max())
+    assert np.allclose(ds, dsigma, rtol=1e-13, atol=1e-13 * np.abs(dsigma).max())
+
+
 def test_adjoint_matches_central_differences(setup):
     _, _, _, _, model = setup
     theta = np.array([0.25, -0.1, 91.187, 2.49])
