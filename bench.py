@@ -234,6 +234,17 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
         out["ratio_vs_fp64"] = value / fp64_value
     else:
         del out["ratio_vs_fp64"]
+    if not args.only:
+        # end to end through the public API (tp_run_batches: host output
+        # arrays, their copies in the timed region)
+        acc = tp.BatchAccumulators(nb)
+        ctx.run_batches(cfg, first32, nb, rng="xoshiro", seed=SEED, precision=tp.TP_PREC_FP32_MIXED, out=acc)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.run_batches(cfg, first32, nb, rng="xoshiro", seed=SEED, precision=tp.TP_PREC_FP32_MIXED, out=acc)
+        e2e_s = time.perf_counter() - t0
+        out["e2e"] = {"value": world * ev32 * args.steps / e2e_s, "unit": "events/s",
+                      "h2d_bytes_per_step": ctypes.sizeof(tp.CConfig), "d2h_bytes_per_step": nb * 13 * 8}
     # roofline: t_min per event = max(W / P_fp32, N_sfu / P_sfu), with the
     # canonical FP work W and special-function count N of an event and the
     # FFMA and MUFU rates measured in this run (tp_probe_fp32)
