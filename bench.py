@@ -171,7 +171,7 @@ def issue_roofline(torch, dev, fp32, clocks):
     """The FP32-mixed kernel is issue-bound (no pipe saturated): its second
     roofline is warp instructions issued per second against the schedulers'
     ceiling (4 per SM per clock at the SM clock sampled in this run). The
-    instructions per event of this build come from its ncu capture
+    kernel's warp instructions per event come from its ncu capture
     (profiles/issue.json); the rate is this run's."""
     path = os.path.join(ROOT, "profiles", "issue.json")
     if not os.path.exists(path) or not clocks.get("sm_mhz") or "kernel_events_per_s" not in fp32:
