@@ -24,10 +24,18 @@ def setup(tp, ctx, cfg_sqrts1000):
     return bins, data_cfg, data, model_cfg, model
 
 
-def test_binned_forward_matches_restatement(tp, oracle, ctx, cfg_sqrts1000):
+@pytest.mark.parametrize("ept", [40, 105, 313])
+def test_binned_forward_matches_restatement(tp, oracle, cfg_sqrts1000, ept):
+    """At 40 events per thread one batch fills a CTA; at 105 and 313 the CTA
+    runs 2 and 8 batches at a time into its shared histogram."""
     cfg = cfg_sqrts1000.replace(num_events=200_000)
     bins = tp.binning(20, 20)
-    gpu = ctx.binned_forward(cfg, 0, cfg.num_batches, bins, SEED_MODEL)
+    with tp.Context(0) as ctx:
+        ctx.set_events_per_thread(ept)
+        gpu = ctx.binned_forward(cfg, 0, cfg.num_batches, bins, SEED_MODEL)
+        # the binned total is the cross-section sum of the batch path
+        acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", seed=SEED_MODEL)
+    assert abs(gpu[:, 6].sum() - acc.sigma.sum()) <= 1e-12 * abs(acc.sigma.sum())
     e = cfg.e_total
     ref = oracle.binned(cfg, tp.rng_flags("xoshiro"), SEED_MODEL, 0, cfg.num_batches, 20, 20, (e / 3, e / 2),
                         (-cfg.beam_photons_cut, cfg.beam_photons_cut))
@@ -40,9 +48,6 @@ def test_binned_forward_matches_restatement(tp, oracle, ctx, cfg_sqrts1000):
     assert np.all(np.abs(m_gpu - ref[:, :5]).sum(axis=0) <= 1e-11 * tot)
     assert np.allclose(gpu[:, 6], ref[:, 6], rtol=1e-11, atol=1e-11 * np.abs(ref[:, 6]).max())
     assert np.allclose(gpu[:, 7], ref[:, 7], rtol=1e-11, atol=1e-11 * np.abs(ref[:, 7]).max())
-    # and the binned total is the cross-section sum of the batch path
-    acc = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", seed=SEED_MODEL)
-    assert abs(gpu[:, 6].sum() - acc.sigma.sum()) <= 1e-12 * abs(acc.sigma.sum())
 
 
 @pytest.mark.parametrize("theta", [(0.0, 0.0, 91.187, 2.49), (0.25, -0.1, 91.187, 2.49), (1.0, 1.0, 91.0, 2.6)])
@@ -81,6 +86,24 @@ def test_adjoint_matches_central_differences(setup):
         fd, fds = (lp - lm) / (2 * h), (sp - sm) / (2 * h)
         assert abs(fd - grad[i]) <= 1e-5 * max(abs(grad[i]), 1e-3 * np.abs(grad).max()), (i, fd, grad[i])
         assert abs(fds - dsigma[i]) <= 1e-5 * max(abs(dsigma[i]), 1e-3 * np.abs(dsigma).max()), (i, fds, dsigma[i])
+
+
+def test_adjoint_shape_invariance(tp, setup):
+    """The adjoint sums do not depend on the block shape (events per thread):
+    multi-warp CTAs at 40, one-warp CTAs at 313."""
+    bins, _, _, _, model = setup
+    theta = (0.25, -0.1, 91.187, 2.49)
+    cfg = model.theta_cfg(theta)
+    _, _, mu = model.value(theta)
+    r = -(mu - model.data) / model.var
+    out = []
+    for ept in (40, 313):
+        with tp.Context(0) as c:
+            c.set_events_per_thread(ept)
+            out.append(c.binned_adjoint(cfg, 0, model.n_batches, bins, r, model.seed, model.precision))
+    (g1, s1), (g2, s2) = out
+    assert np.allclose(g1, g2, rtol=1e-12, atol=1e-12 * np.abs(g1).max())
+    assert np.allclose(s1, s2, rtol=1e-12, atol=1e-12 * np.abs(s1).max())
 
 
 def test_fp32_adjoint_close_to_fp64(tp, setup):

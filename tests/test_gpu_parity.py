@@ -134,13 +134,15 @@ def test_deterministic(ctx, cfg_valeurs):
     assert a.as_array().tobytes() == b.as_array().tobytes()
 
 
+@pytest.mark.parametrize("ept", [80, 313])
 @pytest.mark.parametrize("precision,occ", [(0, 2), (0, 3), (1, 2), (1, 3), (1, 4)])
-def test_kernel_variants(tp, oracle, cfg_valeurs, precision, occ):
-    """Both register/occupancy variants of the xoshiro event kernels."""
+def test_kernel_variants(tp, oracle, cfg_valeurs, precision, occ, ept):
+    """The register/occupancy variants of the xoshiro event kernels, in
+    multi-warp (80 events per thread) and one-warp (313) CTAs."""
     cfg = cfg_valeurs.replace(num_events=60_001)
     with tp.Context(0) as c:
         c.set_occupancy(precision, occ)
-        c.set_events_per_thread(80)
+        c.set_events_per_thread(ept)
         gpu = c.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", precision=precision)
     ref = oracle.run_batches(cfg, 0, cfg.num_batches, tp.rng_flags("xoshiro"), tp.XOSHIRO_DEFAULT_SEED)
     if precision == tp.TP_PREC_FP64:
@@ -150,7 +152,7 @@ def test_kernel_variants(tp, oracle, cfg_valeurs, precision, occ):
         assert rel(gpu.sigma, ref.sigma) < 1e-6
 
 
-@pytest.mark.parametrize("ept", [40, 41, 64, 100, 333, 10000])
+@pytest.mark.parametrize("ept", [40, 41, 64, 100, 313, 333, 10000])
 def test_events_per_thread_invariance(tp, oracle, cfg_valeurs, ept):
     cfg = cfg_valeurs.replace(num_events=30_000)
     with tp.Context(0) as c:
