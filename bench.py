@@ -552,6 +552,17 @@ def main():
         if "bytes_per_event" in tr:
             traffic = tr["bytes_per_event"] * events_per_launch
 
+    # HBM for scale: the kernel's DRAM traffic per launch (ncu) over its
+    # launch time, against the measured copy bandwidth of this GPU model
+    hbm = None
+    ppath = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if traffic is not None and os.path.exists(ppath):
+        hbm_gbs = json.load(open(ppath)).get("hbm_gbs")
+        if hbm_gbs:
+            got = traffic / (launch_ms * 1e-3) / 1e9
+            hbm = {"achieved": got, "peak": hbm_gbs, "unit": "GB/s", "frac": got / hbm_gbs,
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
     # end to end through the public API: host output arrays, copies included
     acc = tp.BatchAccumulators(nb)
     ctx.run_batches(cfg, first, nb, rng="xoshiro", seed=SEED, out=acc)
@@ -584,7 +595,7 @@ def main():
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "DFMA throughput measured in this run (tp_probe_fp64)",
                      "kernel": "k_events_xoshiro_fp64", "flops_per_event": w, "f_acc": f_acc,
-                     "dfma_cost": {k: v for k, v in costs.items() if k != "dfma_flops"}},
+                     "dfma_cost": {k: v for k, v in costs.items() if k != "dfma_flops"}, "hbm": hbm},
         "e2e": e2e,
         "gpu_launches": int(ev_launches + seed_launches),
         "kernel_ms": {"events": ev_ms / args.steps, "seed": seed_ms / args.steps},
