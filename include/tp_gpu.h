@@ -212,9 +212,10 @@ int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
 
 /* Tuning: the xoshiro event kernel variant of `precision`, compiled for 2
- * (default), 3 or (FP32-mixed only) 4 resident CTAs of 256 threads per SM
- * (fewer registers per thread, more warps to hide latency). Results are the
- * same either way. */
+ * (default), 3 or (FP32-mixed only) 4 resident CTAs of 256 threads per SM:
+ * at most 128, 80 or 64 registers per thread (fewer registers, more
+ * resident warps to hide latency, whatever the block shape). Results are
+ * the same either way. */
 int tp_set_occupancy(tp_ctx *ctx, int precision, int min_ctas_per_sm);
 
 /* Tuning in use for `precision`: events per thread and kernel variant
