@@ -127,6 +127,19 @@ def test_golden_run(tp, ctx, cfg_valeurs, features, rng, jump, sort):
     assert compare(res.report(), gold_out[gold_out.index("IBegin"):], rel_tol=1e-12) == []
 
 
+@pytest.mark.parametrize("cfg_name", ["cfg_valeurs", "cfg_sqrts1000"])
+def test_photon_order_symmetry(tp, ctx, request, cfg_name):
+    """Without the plane cut the cuts and the helicity sums are symmetric
+    under permutations of the photons: sorted and unsorted runs select the
+    same events and agree to rounding (the FP32-mixed kernels rely on it and
+    leave the photons unsorted)."""
+    cfg = request.getfixturevalue(cfg_name).replace(num_events=200_000)
+    assert cfg.beam_photon_plane_cut <= 0.0
+    a = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro")
+    b = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro", sorting=False)
+    assert_batches_close(a, b, tol=1e-13)
+
+
 def test_deterministic(ctx, cfg_valeurs):
     cfg = cfg_valeurs.replace(num_events=200_000)
     a = ctx.run_batches(cfg, 0, cfg.num_batches, rng="xoshiro")
