@@ -96,6 +96,7 @@ struct tp_ctx {
   uint32_t* d_ranf_tab = nullptr;
   uint32_t* d_ranf_blocks = nullptr;  // x^(55 D), D < kRanfBlocksInBatch (built on first ranf run)
   uint64_t* d_thread_poly[2] = {nullptr, nullptr};  // per precision: x^(12 ept j), j < 256
+  uint64_t* d_jump_tab[2] = {nullptr, nullptr};     // per precision: the same jumps as tables (8 MiB)
   int thread_poly_ept[2] = {0, 0};
   int32_t* d_ranf_window = nullptr;
   int64_t ranf_window_seed = -1;
@@ -184,6 +185,8 @@ int ensure_thread_poly(tp_ctx* c, int pi) {
   int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[pi], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
                    "upload thread polynomials");
   if (st) return st;
+  if (launch_build_jump_tab(c->d_thread_poly[pi], kTpb, c->d_jump_tab[pi], c->stream) != TP_OK)
+    return c->fail(TP_ERR_CUDA, "building the thread jump tables failed");
   st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
   if (st == TP_OK) c->thread_poly_ept[pi] = ept;
   return st;
@@ -289,6 +292,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
       if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
   kp.thread_poly = c->d_thread_poly[pi];
+  kp.jump_tab = c->d_jump_tab[pi];
   kp.ranf_table = c->d_ranf_tab;
   kp.ranf_blocks = c->d_ranf_blocks;
   if (extra) {
@@ -634,6 +638,8 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
   alloc((void**)&c->d_thread_poly[0], kTpb * 32, "tables");
   alloc((void**)&c->d_thread_poly[1], kTpb * 32, "tables");
+  alloc((void**)&c->d_jump_tab[0], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
+  alloc((void**)&c->d_jump_tab[1], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
@@ -669,7 +675,7 @@ void tp_destroy(tp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly[0], c->d_thread_poly[1],
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly[0], c->d_thread_poly[1], c->d_jump_tab[0], c->d_jump_tab[1],
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
@@ -888,6 +894,7 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   pp.unit_state = reinterpret_cast<uint64_t*>(base + o_us);
   pp.batch_table = c->d_xo_batch;
   pp.thread_poly = c->d_thread_poly[pi];
+  pp.jump_tab = c->d_jump_tab[pi];
   pp.counter = reinterpret_cast<unsigned long long*>(base + o_cnt);
   pp.recheck_count = c->d_recheck;
   auto* sel = reinterpret_cast<uint64_t*>(base + o_out);

@@ -68,6 +68,7 @@ struct KParams {
   int precision;
   const void* batch_state;     // xoshiro: 4 x u64 per batch; ranf: 56 x i32
   const uint64_t* thread_poly; // xoshiro: x^(12 ept j) mod P, 4 words per j
+  const uint64_t* jump_tab;    // xoshiro: the same jumps as tables (kJumpTabWords per j), or null
   const uint32_t* ranf_table;  // ranf: x^(55 2^k) mod P, 55 coefficients per k
   const uint32_t* ranf_blocks; // ranf: x^(55 D) mod P for D < kRanfBlocksInBatch
   BatchOut out;
@@ -93,6 +94,7 @@ struct PointsParams {
   const uint32_t* unit_point;       // [n_units]
   const uint64_t* batch_table;      // 64 x 4: x^(12e4 * 2^k)
   const uint64_t* thread_poly;      // x^(12 ept j)
+  const uint64_t* jump_tab;         // the same as tables, or null
   uint64_t* unit_state;             // [n_units][4] scratch: batch start states
   unsigned long long* counter;      // work-queue head, 0 at launch
   unsigned long long* recheck_count;
@@ -189,6 +191,11 @@ void set_thread_error(const char* msg);
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
 int launch_binned(const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);
+// Four-Russians tables of a thread's xoshiro jump J(T): for each group g of
+// 4 state bits (64 groups) and each value v of the group, the XOR of the
+// images J(T) e_i of the group's set bits: 64 x 16 entries of 4 words.
+constexpr int kJumpTabWords = 64 * 16 * 4;
+int launch_build_jump_tab(const uint64_t* d_poly, int n_threads, uint64_t* d_tab, void* stream);
 int points_grid(int precision, int occupancy, int tpb);  // persistent grid size on the current device
 int events_wave(int precision, int occupancy, int tpb);  // resident xoshiro event CTAs on the current device
 int launch_adjoint(const KParams& p, int tpb, void* stream);
