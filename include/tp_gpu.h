@@ -24,8 +24,9 @@
  *    tp_last_error();
  *  - one context per host thread; calls are synchronous unless their name
  *    ends in _async;
- *  - device memory is owned by the context, host output buffers by the
- *    caller.
+ *  - device memory is owned by the context (about 35 MiB of tables and
+ *    scratch at creation, more for large ranges, binned passes and
+ *    faster-evgen), host output buffers by the caller.
  */
 #ifndef TP_GPU_H
 #define TP_GPU_H
