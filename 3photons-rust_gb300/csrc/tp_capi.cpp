@@ -31,6 +31,7 @@ namespace {
 constexpr uint64_t kChunk = 1ull << 16;
 constexpr int kTpb = 256;      // threads per CTA (one batch per CTA)
 constexpr int kDefaultEpt = 40;  // xoshiro: events per thread (250 x 40)
+constexpr int kBinnedEpt = 313;  // binned passes: one warp per batch (measured fastest for both)
 
 struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
@@ -88,16 +89,18 @@ struct tp_ctx {
   std::string err;
   // per precision (FP64, FP32-mixed): xoshiro events per thread and event
   // kernel variant (min CTAs per SM)
-  int ept[2] = {kDefaultEpt, kDefaultEpt};
+  // [2]: the binned forward and adjoint passes (their own shape: one-warp
+  // batches, eight per CTA in the forward pass; not autotuned)
+  int ept[3] = {kDefaultEpt, kDefaultEpt, kBinnedEpt};
   int occupancy[2] = {2, 2};
   uint64_t* d_xo_batch = nullptr;
   uint64_t* d_xo_jump = nullptr;
   uint64_t* d_xo_draw = nullptr;
   uint32_t* d_ranf_tab = nullptr;
   uint32_t* d_ranf_blocks = nullptr;  // x^(55 D), D < kRanfBlocksInBatch (built on first ranf run)
-  uint64_t* d_thread_poly[2] = {nullptr, nullptr};  // per precision: x^(12 ept j), j < 256
-  uint64_t* d_jump_tab[2] = {nullptr, nullptr};     // per precision: the same jumps as tables (8 MiB)
-  int thread_poly_ept[2] = {0, 0};
+  uint64_t* d_thread_poly[3] = {nullptr, nullptr, nullptr};  // per ept slot: x^(12 ept j), j < 256
+  uint64_t* d_jump_tab[3] = {nullptr, nullptr, nullptr};     // the same jumps as tables (8 MiB each)
+  int thread_poly_ept[3] = {0, 0, 0};
   int32_t* d_ranf_window = nullptr;
   int64_t ranf_window_seed = -1;
   void* d_state = nullptr;
@@ -172,9 +175,11 @@ int ensure(tp_ctx* c, void** p, size_t* have, size_t need, const char* what) {
 
 int prec_index(int precision) { return precision == TP_PREC_FP32_MIXED ? 1 : 0; }
 
-int ensure_thread_poly(tp_ctx* c, int pi) {
-  const int ept = c->ept[pi];
-  if (c->thread_poly_ept[pi] == ept) return TP_OK;
+// Thread jump polynomials and tables of ept slot `slot` (0 FP64, 1
+// FP32-mixed, 2 the binned passes) for its current events per thread.
+int ensure_thread_poly(tp_ctx* c, int slot) {
+  const int ept = c->ept[slot];
+  if (c->thread_poly_ept[slot] == ept) return TP_OK;
   std::vector<uint64_t> h(4 * kTpb);
   const Gf2Poly step = gf2_xpow((uint64_t)kDrawsPerEvent * ept);
   Gf2Poly cur{{1, 0, 0, 0}};
@@ -182,13 +187,13 @@ int ensure_thread_poly(tp_ctx* c, int pi) {
     for (int w = 0; w < 4; ++w) h[4 * j + w] = cur.w[w];
     cur = gf2_mulmod(cur, step);
   }
-  int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[pi], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
+  int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[slot], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
                    "upload thread polynomials");
   if (st) return st;
-  if (launch_build_jump_tab(c->d_thread_poly[pi], kTpb, c->d_jump_tab[pi], c->stream) != TP_OK)
+  if (launch_build_jump_tab(c->d_thread_poly[slot], kTpb, c->d_jump_tab[slot], c->stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, "building the thread jump tables failed");
   st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
-  if (st == TP_OK) c->thread_poly_ept[pi] = ept;
+  if (st == TP_OK) c->thread_poly_ept[slot] = ept;
   return st;
 }
 
@@ -281,18 +286,19 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
   // shape: its per-CTA shared histogram (up to 96 KB) limits how many CTAs
   // fit on an SM
   const int pi = prec_index(precision);
-  const int ept = c->ept[pi];
+  const int slot = (pass == Pass::kBinned || pass == Pass::kAdjoint) ? 2 : pi;
+  const int ept = c->ept[slot];
   kp.ept = ept;
   kp.occupancy = c->occupancy[pi];
   if (kind == TP_RNG_XOSHIRO256P) {
-    if (int st = ensure_thread_poly(c, pi)) return st;
+    if (int st = ensure_thread_poly(c, slot)) return st;
   } else {
     if (int st = ensure_ranf_blocks(c)) return st;
     if (!jpb)
       if (int st = ensure_ranf_window(c, (int32_t)seed)) return st;
   }
-  kp.thread_poly = c->d_thread_poly[pi];
-  kp.jump_tab = c->d_jump_tab[pi];
+  kp.thread_poly = c->d_thread_poly[slot];
+  kp.jump_tab = c->d_jump_tab[slot];
   kp.ranf_table = c->d_ranf_tab;
   kp.ranf_blocks = c->d_ranf_blocks;
   if (extra) {
@@ -636,10 +642,10 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_xo_jump, 256 * 8, "tables");
   alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
   alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
-  alloc((void**)&c->d_thread_poly[0], kTpb * 32, "tables");
-  alloc((void**)&c->d_thread_poly[1], kTpb * 32, "tables");
-  alloc((void**)&c->d_jump_tab[0], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
-  alloc((void**)&c->d_jump_tab[1], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
+  for (int k = 0; k < 3; ++k) {
+    alloc((void**)&c->d_thread_poly[k], kTpb * 32, "tables");
+    alloc((void**)&c->d_jump_tab[k], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
+  }
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");
@@ -675,7 +681,9 @@ void tp_destroy(tp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks, c->d_thread_poly[0], c->d_thread_poly[1], c->d_jump_tab[0], c->d_jump_tab[1],
+  void* bufs[] = {c->d_xo_batch, c->d_xo_jump, c->d_xo_draw, c->d_ranf_tab, c->d_ranf_blocks,
+                  c->d_thread_poly[0], c->d_thread_poly[1], c->d_thread_poly[2],
+                  c->d_jump_tab[0], c->d_jump_tab[1], c->d_jump_tab[2],
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
                   c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
@@ -771,7 +779,7 @@ int tp_dump_events_prec(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t 
 int tp_set_events_per_thread(tp_ctx* c, int ept) {
   if (!c) return TP_ERR_INVALID;
   if (ept <= 0 || (TP_BATCH_SIZE + ept - 1) / ept > kTpb) return c->fail(TP_ERR_INVALID, "events per thread out of range");
-  c->ept[0] = c->ept[1] = ept;
+  c->ept[0] = c->ept[1] = c->ept[2] = ept;
   return TP_OK;
 }
 

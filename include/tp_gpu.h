@@ -24,7 +24,7 @@
  *    tp_last_error();
  *  - one context per host thread; calls are synchronous unless their name
  *    ends in _async;
- *  - device memory is owned by the context (about 35 MiB of tables and
+ *  - device memory is owned by the context (about 45 MiB of tables and
  *    scratch at creation, more for large ranges, binned passes and
  *    faster-evgen), host output buffers by the caller.
  */
@@ -208,7 +208,8 @@ int tp_dump_events_prec(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
                         int precision, tp_event_dump *out);
 
 /* Tuning: events each thread integrates in the xoshiro kernels, for both
- * precisions (default 40; ceil(10000 / ept) must not exceed 256). No
+ * precisions and the binned passes (defaults: 40 for the event kernels,
+ * 313 for the binned passes; ceil(10000 / ept) must not exceed 256). No
  * counterpart in the reference, whose batches run on one CPU thread each. */
 int tp_set_events_per_thread(tp_ctx *ctx, int ept);
 
