@@ -99,7 +99,7 @@ struct tp_ctx {
   uint32_t* d_ranf_tab = nullptr;
   uint32_t* d_ranf_blocks = nullptr;  // x^(55 D), D < kRanfBlocksInBatch (built on first ranf run)
   uint64_t* d_thread_poly[3] = {nullptr, nullptr, nullptr};  // per ept slot: x^(12 ept j), j < 256
-  uint64_t* d_jump_tab[3] = {nullptr, nullptr, nullptr};     // the same jumps as tables (8 MiB each)
+  uint64_t* d_jump_tab[3] = {nullptr, nullptr, nullptr};     // the same jumps as tables (8 MiB; not slot 2)
   int thread_poly_ept[3] = {0, 0, 0};
   int32_t* d_ranf_window = nullptr;
   int64_t ranf_window_seed = -1;
@@ -190,7 +190,7 @@ int ensure_thread_poly(tp_ctx* c, int slot) {
   int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[slot], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
                    "upload thread polynomials");
   if (st) return st;
-  if (launch_build_jump_tab(c->d_thread_poly[slot], kTpb, c->d_jump_tab[slot], c->stream) != TP_OK)
+  if (c->d_jump_tab[slot] && launch_build_jump_tab(c->d_thread_poly[slot], kTpb, c->d_jump_tab[slot], c->stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, "building the thread jump tables failed");
   st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
   if (st == TP_OK) c->thread_poly_ept[slot] = ept;
@@ -642,10 +642,9 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_xo_jump, 256 * 8, "tables");
   alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
   alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
-  for (int k = 0; k < 3; ++k) {
-    alloc((void**)&c->d_thread_poly[k], kTpb * 32, "tables");
-    alloc((void**)&c->d_jump_tab[k], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
-  }
+  // the binned passes (slot 2) jump by polynomial: no table
+  for (int k = 0; k < 3; ++k) alloc((void**)&c->d_thread_poly[k], kTpb * 32, "tables");
+  for (int k = 0; k < 2; ++k) alloc((void**)&c->d_jump_tab[k], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
   alloc((void**)&c->d_ranf_window, 110 * 4, "tables");
   alloc((void**)&c->d_err, sizeof(unsigned int), "error word");
   alloc((void**)&c->d_recheck, sizeof(unsigned long long), "recheck counter");

@@ -24,7 +24,7 @@
  *    tp_last_error();
  *  - one context per host thread; calls are synchronous unless their name
  *    ends in _async;
- *  - device memory is owned by the context (about 45 MiB of tables and
+ *  - device memory is owned by the context (about 35 MiB of tables and
  *    scratch at creation, more for large ranges, binned passes and
  *    faster-evgen), host output buffers by the caller.
  */
