@@ -190,7 +190,8 @@ int ensure_thread_poly(tp_ctx* c, int slot) {
   int st = c->cuda(cudaMemcpyAsync(c->d_thread_poly[slot], h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->stream),
                    "upload thread polynomials");
   if (st) return st;
-  if (c->d_jump_tab[slot] && launch_build_jump_tab(c->d_thread_poly[slot], kTpb, c->d_jump_tab[slot], c->stream) != TP_OK)
+  if (c->d_jump_tab[slot] &&
+      launch_build_jump_tab(c->d_thread_poly[slot], kTpb, c->d_jump_tab[slot], c->stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, "building the thread jump tables failed");
   st = c->cuda(cudaStreamSynchronize(c->stream), "upload thread polynomials");
   if (st == TP_OK) c->thread_poly_ept[slot] = ept;
