@@ -214,7 +214,8 @@ def _ptr(a):
 
 # ---- Configuration (src/config.rs) ----------------------------------------
 class Configuration:
-    """The 18 items of `valeurs` (src/config.rs:152-198)."""
+    """The 18 items of `valeurs` (src/config.rs:8-53, read by
+    Configuration::load, src/config.rs:57-128)."""
 
     FIELDS = [f for f, _ in CConfig._fields_ if f != "reserved"]
 

@@ -348,7 +348,7 @@ int tp_config_load(const char* path, tp_config* out, char* echo, size_t echo_len
     copy_out(s, echo, echo_len);
   }
   *out = c;
-  // the reference echoes first, then applies its checks (src/config.rs:256-269)
+  // the reference echoes first, then applies its checks (src/config.rs:110-124)
   if (c.num_events == 0 || c.plot || c.impr) return TP_ERR_INVALID;
   return TP_OK;
 }

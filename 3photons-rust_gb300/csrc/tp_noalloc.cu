@@ -1,14 +1,13 @@
 // tp_noalloc.cu — tp_run_batches_noalloc: the batch event loop for callers
 // that must not allocate GPU memory.
 //
-// Some hosts cannot call cudaMalloc at the moment they want events: code
-// that runs while a CUDA graph is being captured, real-time or embedded
-// callers whose memory is planned once at start-up, or programs whose GPU
-// memory belongs to another allocator (a framework's caching pool) that the
-// library must not bypass. This entry point serves them: it needs no
-// tp_ctx, calls no cudaMalloc/cudaFree, and keeps its only working memory
-// in the fixed arrays below, which exist on every GPU that loads the
-// library for as long as the process lives.
+// Some hosts cannot call cudaMalloc at the moment they want events:
+// real-time or embedded callers whose GPU memory is planned once at
+// start-up, or programs whose GPU memory belongs to another allocator (a
+// framework's caching pool) that the library must not bypass. This entry
+// point serves them: it needs no tp_ctx, calls no cudaMalloc/cudaFree, and
+// keeps its only working memory in the fixed arrays below, which exist on
+// every GPU that loads the library for as long as the process lives.
 //
 // Working memory: the start state of every batch of the call (the scratch
 // written by the seeding kernel and read by the event kernel), plus the
@@ -37,8 +36,9 @@ static __device__ __align__(256) uint64_t g_noalloc_tables[4 * 384];
 
 struct DeviceSetup {
   bool ready = false;
-  uint64_t* state = nullptr;   // device address of g_noalloc_state
-  uint64_t* tables = nullptr;  // device address of g_noalloc_tables
+  unsigned long long ctx_id = 0;  // the CUDA context the addresses belong to
+  uint64_t* state = nullptr;      // device address of g_noalloc_state
+  uint64_t* tables = nullptr;     // device address of g_noalloc_tables
 };
 
 constexpr int kMaxDevices = 64;
@@ -50,18 +50,49 @@ int fail(int code, const char* msg) {
   return code;
 }
 
-// Once per device, with that device current: look up the arrays' device
-// addresses and upload the jump polynomials (a plain copy into the fixed
-// array; nothing is allocated).
+// The process-unique ID of the current CUDA context (cuCtxGetId through
+// the runtime's driver entry points, so the library links no driver
+// library), or 0 when it cannot be read. A cudaDeviceReset followed by new
+// work gives the device a new primary context with a new ID, whose copy of
+// the fixed arrays has not been set up.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Once per device and context, with that device current: look up the
+// arrays' device addresses and upload the jump polynomials (a plain copy
+// into the fixed array; nothing is allocated). The lookup also makes the
+// device's primary context current on this thread.
 int setup_device(int dev, DeviceSetup** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   DeviceSetup& d = g_setup[dev];
-  if (!d.ready) {
-    void* state = nullptr;
-    void* tables = nullptr;
-    if (cudaGetSymbolAddress(&state, g_noalloc_state) != cudaSuccess ||
-        cudaGetSymbolAddress(&tables, g_noalloc_tables) != cudaSuccess)
-      return fail(TP_ERR_CUDA, "tp_run_batches_noalloc: cudaGetSymbolAddress failed on this device");
+  void* state = nullptr;
+  void* tables = nullptr;
+  if (cudaGetSymbolAddress(&state, g_noalloc_state) != cudaSuccess ||
+      cudaGetSymbolAddress(&tables, g_noalloc_tables) != cudaSuccess)
+    return fail(TP_ERR_CUDA, "tp_run_batches_noalloc: cudaGetSymbolAddress failed on this device");
+  const unsigned long long ctx_id = current_context_id();
+  if (!d.ready || (ctx_id != 0 && ctx_id != d.ctx_id) || state != d.state || tables != d.tables) {
+    d.ready = false;
     uint64_t host[4 * 384];
     Gf2Poly pb = gf2_xpow(kDrawsPerBatch), pj = gf2_xpow2k(128);
     for (int k = 0; k < 64; ++k) {
@@ -82,6 +113,7 @@ int setup_device(int dev, DeviceSetup** out) {
       return fail(TP_ERR_CUDA, "tp_run_batches_noalloc: uploading the jump tables failed");
     d.state = static_cast<uint64_t*>(state);
     d.tables = static_cast<uint64_t*>(tables);
+    d.ctx_id = ctx_id;
     d.ready = true;
   }
   *out = &d;

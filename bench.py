@@ -42,8 +42,11 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
 METRIC = "events/s on 1 GB300: FP32-mixed vs FP64 plain at sigma rel.err<=1e-6; grad/fwd time"
 
 
+WORKLOAD_VALEURS = os.path.join(ROOT, "tests", "golden", "valeurs_sqrts1000")
+
+
 def workload_config(tp, events):
-    cfg = tp.Configuration.load(os.path.join(ROOT, "tests", "golden", "valeurs_sqrts1000"), echo=False)
+    cfg = tp.Configuration.load(WORKLOAD_VALEURS, echo=False)
     return cfg.replace(num_events=events)
 
 
@@ -111,14 +114,24 @@ def algorithmic_flops_per_event(f_acc, costs):
     return w
 
 
-def cpu_baseline(tp, events_budget_s=3.0):
-    """The CPU restatement (FP64, the same xoshiro stream and physics) on all
-    host cores over a bounded sample of the workload's first batches."""
+def oracle_workload(tp, events):
+    """The CPU restatement and the workload configuration parsed by the
+    restatement's own `valeurs` reader: the reference arm maps no product
+    library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import tp_oracle_py
 
     oracle = tp_oracle_py.Oracle(tp)
-    cfg = workload_config(tp, WORKLOAD_EVENTS)
+    st, cfg, _ = oracle.load(WORKLOAD_VALEURS)
+    if st != 0:
+        raise RuntimeError("cannot read %s (%d)" % (WORKLOAD_VALEURS, st))
+    return oracle, cfg.replace(num_events=events)
+
+
+def cpu_baseline(tp, events_budget_s=3.0):
+    """The CPU restatement (FP64, the same xoshiro stream and physics) on all
+    host cores over a bounded sample of the workload's first batches."""
+    oracle, cfg = oracle_workload(tp, WORKLOAD_EVENTS)
     threads = os.cpu_count() or 1
     kind = tp.rng_flags("xoshiro")
     nb = max(threads, 8)
@@ -139,6 +152,104 @@ def cpu_baseline(tp, events_budget_s=3.0):
             "value_1core": nb1 * tp.TP_BATCH_SIZE / dt1,
             "sample": "first %d batches (%d events) of the workload, FP64, %d threads; one core: first %d batches"
                       % (nb, ev, threads, nb1)}
+
+
+# DFMA-equivalent cost of CUDA 13.0's own FP64 log, sincos, sqrt and
+# division on GB300, measured once (8 independent chains per thread at full
+# occupancy against 16-chain DFMA, the method of tp_probe_fp64) and frozen
+# here, so that a cheaper implementation in the kernel raises frac_fixed
+# instead of lowering the work it is credited with.
+FROZEN_LIBM_COST = {"log": None, "sincos": 24.9, "sqrt": 8.6, "div": 8.6}
+
+
+def fixed_fp64_fraction(torch, dev, f_acc, kernel_events_per_s, clocks):
+    """The FP64 roofline with every weight fixed: the canonical work of an
+    event with each library call at CUDA's own cost (FROZEN_LIBM_COST),
+    against the nominal FP64 peak of the GPU, 2 DFMA (4 flops) per clock and
+    SM, at the SM clock sampled during the timed region."""
+    if FROZEN_LIBM_COST["log"] is None or not clocks.get("sm_mhz"):
+        return None
+    w = algorithmic_flops_per_event(f_acc, FROZEN_LIBM_COST)
+    peak = 4.0 * torch.cuda.get_device_properties(dev).multi_processor_count * clocks["sm_mhz"] * 1e6
+    return {"frac": w * kernel_events_per_s / peak, "flops_per_event": w, "peak_tflops": peak / 1e12,
+            "weights": dict(FROZEN_LIBM_COST), "peak_source": "nominal 2 DFMA/clock/SM at the sampled SM clock"}
+
+
+def sig(x, n=5):
+    """x with floats rounded to n significant digits (recursively)."""
+    if isinstance(x, float):
+        return float("%.*g" % (n, x)) if np.isfinite(x) else None
+    if isinstance(x, dict):
+        return {k: sig(v, n) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [sig(v, n) for v in x]
+    return x
+
+
+def compact_line(d, detail_path=None):
+    """The one JSON line bench.py prints: the contract's keys, the legs'
+    headline figures, and last (so that a tail of the output keeps them)
+    the precision form's events/s, its end-to-end rate, its ratio to the FP64
+    path, its largest res.data error against FP64 and the grad/fwd ratio.
+    Everything else goes to the --detail file."""
+    keep = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+            "vs_baseline", "dtype", "data", "gpu_launches")
+    out = {k: d[k] for k in keep if k in d}
+    c = d["config"]
+    out["config"] = {"workload": "FP64 plain, sqrt(s)=1000 GeV, xoshiro256+ seed 12345 with jump-ahead, 1e9 events "
+                                 "= 1e5 batches of 1e4 per GPU", "l2": c["l2"], "parallelism": c["parallelism"],
+                     "ept": c["autotuned_events_per_thread"], "ctas_per_sm": c["kernel_variant_ctas_per_sm"]}
+    r = d["roofline"]
+    ff = r.get("frac_fixed")
+    out["roofline"] = {"bound": r["bound"], "achieved": r["achieved"], "peak": r["peak"], "unit": r["unit"],
+                       "frac": r["frac"], "traffic": r["traffic"], "kernel": r["kernel"],
+                       "peak_source": "DFMA rate measured in this run",
+                       "frac_fixed": ff["frac"] if ff else None, "fp64_pipe_active_ncu": r.get("fp64_pipe_active_ncu")}
+    if "cpu_baseline" in d:
+        cb = d["cpu_baseline"]
+        out["cpu_baseline"] = {"value": cb["value"], "unit": cb["unit"], "cores": cb["cores"], "kind": cb["kind"],
+                               "value_1core": cb.get("value_1core"), "sample": cb["sample"]}
+    out["clocks"] = d["clocks"]
+    out["e2e"] = d["e2e"]
+    f = d["fp32_mixed"]
+    out["fp32"] = {"kernel": f["kernel"], "kernel_ms": f["kernel_ms"], "ept": f["autotuned_events_per_thread"],
+                   "ctas_per_sm": f["kernel_variant_ctas_per_sm"], "rechecked": f["rechecked_fraction"],
+                   "roofline_frac": f["roofline"]["frac"], "sfu_frac": f["roofline"]["sfu_frac"],
+                   "issue_frac": f["roofline"].get("issue", {}).get("frac"),
+                   "e2e_bytes": [f["e2e"]["h2d_bytes_per_step"], f["e2e"]["d2h_bytes_per_step"]] if "e2e" in f
+                   else None}
+    acc = f.get("accuracy_vs_fp64")
+    if acc:
+        out["fp32"]["selected_equal"] = acc["selected_equal"]
+        out["fp32"]["rel_err"] = {k: acc["rel_err"][k] for k in ("sigma", "beta_min", "spm2_1_A", "spm2_1_B+")}
+    g = d.get("grad")
+    if g:
+        t = g["at_test_point"]
+        out["grad"] = {"forward_ms": g["forward_ms"], "adjoint_ms": g["adjoint_ms"], "theta": t["theta"],
+                       "dlnL_dtheta": t["dlnL_dtheta"], "rel_dev_vs_analytic": t["max_rel_dev_vs_analytic"],
+                       "rel_dev_vs_central_diff": t["max_rel_dev_vs_central_diff"]}
+        if "flipped_bins" in g:
+            out["grad"]["flipped_bins"] = g["flipped_bins"]
+        if "fit" in g:
+            out["grad"]["fit_beta"] = g["fit"]["beta"]
+            out["grad"]["fit_err"] = g["fit"]["beta_err"]
+    for key in ("batched", "ranf"):
+        if key in d:
+            out[key] = {k: v for k, v in d[key].items() if k in ("value", "e2e", "events_per_step", "fp64", "fp32",
+                                                                 "fp32_over_xoshiro")}
+    if "faster_evgen" in d:
+        out["faster_evgen"] = {x["rng"]: {"events_per_s": x["events_per_s"], "boundary_ms": x["boundary_pass_ms"],
+                                          "ms": x["ms_per_step"]} for x in d["faster_evgen"]}
+    out["detail"] = detail_path
+    out["fp32_mixed_value"] = f["value"]
+    out["fp32_mixed_e2e"] = f["e2e"]["value"] if "e2e" in f else None
+    out["fp32_over_fp64"] = f.get("ratio_vs_fp64")
+    out["fp32_max_rel_err"] = acc["max_rel_err"] if acc else None
+    out["grad_over_fwd"] = g["grad_over_fwd"] if g else None
+    value, e2e = out["value"], dict(out["e2e"])
+    out = sig(out)
+    out["value"], out["e2e"] = value, e2e
+    return out
 
 
 RES_FIELDS = ("sigma", "prec", "beta_min", "ss_p", "inc_ss_p", "ss_m", "inc_ss_m")
@@ -270,6 +381,34 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     return out
 
 
+def gradient_checks(tp, model, theta, h_rel=1e-4):
+    """The adjoint gradient at `theta` (all four components non-zero away
+    from beta+- = 0) against (1) the analytic gradient of the forward pass's
+    per-bin raw sums and (2) central differences (h = 1e-4 max(|theta_i|, 1))
+    of ln L evaluated from the same forward pass's per-bin sums, so both
+    references see the same events. Relative deviations per component."""
+    theta = np.array(theta, np.float64)
+    _, grad, _, dsigma = model.gradient(theta)
+    hist = model.last_hist
+    ga, dsa = model.analytic_gradient(theta, hist)
+
+    def lnl(t):
+        mu = model._mu(hist, model.theta_cfg(t))[0]
+        return -0.5 * float(np.sum((mu - model.data) ** 2 / model.var))
+
+    fd = np.zeros(4)
+    for i in range(4):
+        h = h_rel * max(abs(theta[i]), 1.0)
+        tp_, tm = theta.copy(), theta.copy()
+        tp_[i] += h
+        tm[i] -= h
+        fd[i] = (lnl(tp_) - lnl(tm)) / (2 * h)
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))
+    return {"theta": theta.tolist(), "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": dsigma.tolist(),
+            "max_rel_dev_vs_analytic": rel(grad, ga), "max_rel_dev_dsigma_vs_analytic": rel(dsigma, dsa),
+            "max_rel_dev_vs_central_diff": rel(grad, fd), "central_diff_h_rel": h_rel}
+
+
 def grad_leg(tp, ctx, args, events, fit_steps=200):
     """The differentiation form: a 20 x 20 binned Gaussian log-likelihood of
     a model run (beta+- = 0, M_Z = 91.187, Gamma_Z = 2.490, seed 12345)
@@ -306,6 +445,7 @@ def grad_leg(tp, ctx, args, events, fit_steps=200):
            "adjoint_ms": 1e3 * a, "grad_over_fwd": a / f, "gradient_step_over_fwd": (f + a) / f,
            "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": (flux * s @ dk).tolist(),
            "max_rel_dev_vs_analytic": float(np.max(np.abs(grad - ga)) / np.max(np.abs(ga)))}
+    out["at_test_point"] = gradient_checks(tp, model, (0.25, -0.1, 91.187, 2.49))
     if fit_steps:
         # recover beta+- from the pseudo-data: natural-gradient steps, each a
         # forward and an adjoint pass over all events. Only beta-^2 enters the
@@ -398,12 +538,8 @@ def run_reference(args):
         return
     import __graft_entry__ as graft
 
-    tp = graft.package()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import tp_oracle_py
-
-    oracle = tp_oracle_py.Oracle(tp)
-    cfg = workload_config(tp, WORKLOAD_EVENTS)
+    tp = graft.package()  # ctypes struct layouts and constants only: no library load
+    oracle, cfg = oracle_workload(tp, WORKLOAD_EVENTS)
     threads = os.cpu_count() or 1
     kind = tp.rng_flags("xoshiro")
     nb = 4 * threads
@@ -422,6 +558,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "sqrt(s)=1000 GeV, xoshiro256+ seed 12345, FP64 plain; each step the first "
                                "%d batches (%d events) of the 1e9-event run" % (nb, ev),
+                   "same_config": "same physics, stream and metric; each step the first %d batches of the "
+                                  "workload, not all 1e5 (a bounded CPU sample)" % nb,
                    "events_per_step": ev, "threads": threads},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
                          "sample": "CPU restatement of the reference path (the Rust reference has no toolchain "
@@ -443,6 +581,8 @@ def main():
     ap.add_argument("--occupancy", type=int, default=None, help="with --only: kernel variant, CTAs per SM")
     ap.add_argument("--only", choices=["fp64", "fp32", "fe"], default=None,
                     help="time one leg only (no e2e, no CPU baseline): for profiler captures")
+    ap.add_argument("--detail", default=None,
+                    help="also write every measured quantity (per-quantity errors, fit trace) to this JSON file")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -545,12 +685,13 @@ def main():
     events_per_launch = events * args.steps / max(ev_launches, 1)
     achieved = w * events_per_launch / (launch_ms * 1e-3)
     peak = costs["dfma_flops"]
-    traffic = None
+    traffic = pipe_active = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         tr = json.load(open(tpath))
         if "bytes_per_event" in tr:
             traffic = tr["bytes_per_event"] * events_per_launch
+        pipe_active = tr.get("fp64_pipe_active")
 
     # HBM for scale: the kernel's DRAM traffic per launch (ncu) over its
     # launch time, against the measured copy bandwidth of this GPU model
@@ -595,7 +736,8 @@ def main():
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "DFMA throughput measured in this run (tp_probe_fp64)",
                      "kernel": "k_events_xoshiro_fp64", "flops_per_event": w, "f_acc": f_acc,
-                     "dfma_cost": {k: v for k, v in costs.items() if k != "dfma_flops"}, "hbm": hbm},
+                     "dfma_cost": {k: v for k, v in costs.items() if k != "dfma_flops"}, "hbm": hbm,
+                     "fp64_pipe_active_ncu": pipe_active},
         "e2e": e2e,
         "gpu_launches": int(ev_launches + seed_launches),
         "kernel_ms": {"events": ev_ms / args.steps, "seed": seed_ms / args.steps},
@@ -604,6 +746,8 @@ def main():
         "fp32_mixed": fp32,
     }
     issue_roofline(torch, dev, fp32, line["clocks"])
+    line["roofline"]["frac_fixed"] = fixed_fp64_fraction(torch, dev, f_acc, events_per_launch / (launch_ms * 1e-3),
+                                                         line["clocks"])
     if world == 1:
         line["grad"] = grad_leg(tp, ctx, args, events)
         line["batched"] = points_leg(tp, ctx, args)
@@ -612,7 +756,10 @@ def main():
                                                  tp.RANF_DEFAULT_SEED)]
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(tp)
-    print(json.dumps(line))
+    if args.detail:
+        with open(args.detail, "w") as fh:
+            json.dump(line, fh, indent=1)
+    print(json.dumps(compact_line(line, args.detail)))
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -100,7 +100,8 @@ extern "C" {
 #define TP_PREC_FP32_MIXED 1 /* FP32 event math, FP64 batch sums, FP64
                                 recheck of events near a cut boundary     */
 
-/* ---- configuration: the 18 items of `valeurs` (src/config.rs:152-198) --- */
+/* ---- configuration: the 18 items of `valeurs` (src/config.rs:8-53, read
+ * in file order by Configuration::load, src/config.rs:84-101) ------------- */
 typedef struct tp_config {
   uint64_t num_events;          /* ITOT: total events of the run; also the
                                    normalisation of every event weight
@@ -120,8 +121,8 @@ typedef struct tp_config {
   double beta_plus;             /* anomalous coupling beta+               */
   double beta_minus;            /* anomalous coupling beta-               */
   int32_t num_bins;             /* NBIN (read, unused by the reference)   */
-  int32_t impr;                 /* must be 0 (src/config.rs:265-269)      */
-  int32_t plot;                 /* must be 0 (src/config.rs:260)          */
+  int32_t impr;                 /* must be 0 (src/config.rs:120-124)      */
+  int32_t plot;                 /* must be 0 (src/config.rs:117)          */
   int32_t reserved;             /* keep 0                                 */
 } tp_config;
 
@@ -351,21 +352,27 @@ int tp_ranf_state_at(int32_t seed, uint64_t draws, int32_t slots[55],
 
 /* ---- allocation-free batches -----------------------------------------------
  * No counterpart in the reference. For callers that must not allocate GPU
- * memory when they want events: code running inside a CUDA graph capture,
- * real-time or embedded hosts that plan all memory at start-up, programs
- * whose GPU memory belongs to another allocator. Same work as
- * tp_run_batches_async for the xoshiro256+ stream (rng_kind =
- * TP_RNG_XOSHIRO256P, optionally with TP_MODE_* flags), FP64 or FP32-mixed,
- * on the CURRENT CUDA device and the given stream (a cudaStream_t; NULL is
- * the default stream), writing the caller's DEVICE arrays `out`. No context,
- * no cudaMalloc/cudaFree: the working memory (the start state of each batch
- * and the jump-ahead tables) lives in fixed arrays of the library, 140 KiB
- * per GPU that loads the library, held until the process exits.
+ * memory when they want events: real-time or embedded hosts that plan all
+ * GPU memory at start-up, programs whose GPU memory belongs to another
+ * allocator (a framework's caching pool) that this library must not
+ * bypass. Same work as tp_run_batches_async for the xoshiro256+ stream:
+ * rng_kind = TP_RNG_XOSHIRO256P, optionally OR-ed with
+ * TP_MODE_JUMP_PER_BATCH and/or TP_MODE_NO_PHOTON_SORTING (other flags,
+ * TP_MODE_FASTER_EVGEN included, give TP_ERR_INVALID); FP64 or
+ * FP32-mixed; on the CURRENT CUDA device and the given stream (a
+ * cudaStream_t; NULL is the default stream), writing the caller's DEVICE
+ * arrays `out`. No context, no cudaMalloc/cudaFree: the working memory (the
+ * start state of each batch and the jump-ahead tables) lives in fixed
+ * arrays of the library, 140 KiB per GPU that loads the library, held until
+ * the process exits.
  *  - at most TP_NOALLOC_MAX_BATCHES batches per call; larger ranges fail
- *    with TP_ERR_INVALID: split them into several calls;
+ *    with TP_ERR_INVALID: split them into several calls. Batches at or past
+ *    ceil(num_events / TP_BATCH_SIZE) hold no events and come back with
+ *    zero sums, as in tp_run_batches;
  *  - the first call on a device sets that device up (looks up the arrays'
  *    addresses, uploads the tables with a synchronous copy): make that
- *    first call before any stream capture;
+ *    first call before any stream capture. After a cudaDeviceReset the next
+ *    call sets the device up again (it checks the context's ID);
  *  - every call shares the same working memory, so calls that overlap on
  *    the GPU (other streams, other host threads) race; order them on one
  *    stream or synchronise between them. Nothing in it needs clearing: each

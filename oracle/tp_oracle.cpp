@@ -944,8 +944,12 @@ void tpo_m2_sums_of(const tp_config* cfg, const double* p_out, double out[5]) {
 // event order (skipping to first_batch by stepping), or one jumped stream per
 // batch. threads > 1 runs batches in parallel (batch start states are
 // prepared first by the stepping / jumping the reference's scheduler does).
-int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
-                    tp_batch_soa* out, int threads) {
+// The batches of a run whose stream starts from `seed` jumped `jumps`
+// times by RandomGenerator::jump (xoshiro: 2^128 draws, standard.rs:53-55;
+// ranf: reseeded with seed + 123456 per jump, ranf.rs:137-140). jumps = 0 is
+// the reference's run; jumps = p is one stream per parameter point p.
+static int run_batches_from(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t jumps, uint64_t first_batch,
+                            uint64_t n_batches, tp_batch_soa* out, int threads) {
   if (!cfg_ok(cfg) || !out) return TP_ERR_INVALID;
   const int flags = rng_kind & ~TP_RNG_KIND_MASK;
   const int kind = rng_kind & TP_RNG_KIND_MASK;
@@ -953,6 +957,7 @@ int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
   const Consts k = make_consts(*cfg);
   Rng rng;
   rng.init(kind, seed);
+  for (uint64_t j = 0; j < jumps; ++j) rng.jump();
   // position the stream at first_batch: one-stream default-mode runs by a
   // matrix power (12 draws per event), the others batch by batch
   uint64_t skipped = 0;
@@ -1018,6 +1023,16 @@ int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
     });
   for (auto& th : pool) th.join();
   return TP_OK;
+}
+
+int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
+                    tp_batch_soa* out, int threads) {
+  return run_batches_from(cfg, rng_kind, seed, 0, first_batch, n_batches, out, threads);
+}
+
+int tpo_run_batches_jumped(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t jumps, uint64_t first_batch,
+                           uint64_t n_batches, tp_batch_soa* out, int threads) {
+  return run_batches_from(cfg, rng_kind, seed, jumps, first_batch, n_batches, out, threads);
 }
 
 // Per-bin sums of the kept events of batches [first_batch, first_batch + n):

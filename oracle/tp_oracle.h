@@ -25,6 +25,10 @@ int tpo_dump_events(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t 
 void tpo_m2_sums_of(const tp_config* cfg, const double* p_out, double out[5]);
 int tpo_run_batches(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
                     tp_batch_soa* out, int threads);
+// tpo_run_batches for a stream that starts from `seed` jumped `jumps` times
+// (RandomGenerator::jump): the stream of parameter point `jumps` of a scan.
+int tpo_run_batches_jumped(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t jumps, uint64_t first_batch,
+                           uint64_t n_batches, tp_batch_soa* out, int threads);
 int tpo_binned(const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches, int nx,
                int ny, double xlo, double xhi, double ylo, double yhi, double* out);
 int tpo_merge_finalize(const tp_config* cfg, const tp_batch_soa* b, uint64_t n, tp_final_results* res);

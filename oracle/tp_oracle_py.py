@@ -44,6 +44,7 @@ def lib(pkg):
         L.tpo_dump_events.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, vp]
         L.tpo_m2_sums_of.argtypes = [P(pkg.CConfig), P(ctypes.c_double), P(ctypes.c_double)]
         L.tpo_run_batches.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, P(pkg.CBatchSoa), i32]
+        L.tpo_run_batches_jumped.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, u64, P(pkg.CBatchSoa), i32]
         d = ctypes.c_double
         L.tpo_binned.argtypes = [P(pkg.CConfig), i32, u64, u64, u64, i32, i32, d, d, d, d, vp]
         L.tpo_merge_finalize.argtypes = [P(pkg.CConfig), P(pkg.CBatchSoa), u64, P(pkg.CFinalResults)]
@@ -70,6 +71,16 @@ class Oracle:
         threads = threads or os.cpu_count() or 1
         st = self.L.tpo_run_batches(ctypes.byref(cfg.c), rng_kind, seed, first_batch, n_batches,
                                     ctypes.byref(soa), threads)
+        assert st == 0, st
+        return acc
+
+    def run_batches_jumped(self, cfg, first_batch, n_batches, rng_kind, seed, jumps, threads=None):
+        """Batches of the stream `seed` jumped `jumps` times (a scan's point)."""
+        acc = self.pkg.BatchAccumulators(n_batches)
+        soa = acc.soa()
+        threads = threads or os.cpu_count() or 1
+        st = self.L.tpo_run_batches_jumped(ctypes.byref(cfg.c), rng_kind, seed, jumps, first_batch, n_batches,
+                                           ctypes.byref(soa), threads)
         assert st == 0, st
         return acc
 

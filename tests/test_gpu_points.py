@@ -61,3 +61,26 @@ def test_autotune_keeps_results(tp, cfg_sqrts1000):
     # equal to FP32 accumulation accuracy
     assert np.array_equal(got.selected, ref.selected)
     assert np.allclose(got.sigma, ref.sigma, rtol=1e-6)
+
+
+def test_scan_points_match_restatement(tp, oracle, cfg_sqrts1000):
+    """Points of the benchmark's scan (random sqrt(s), E_min, cuts and
+    beta+-, 1e6 to 1e8 events each) run by the persistent launch against
+    the CPU restatement of the same point: its stream is seed 12345 jumped
+    p times, consumed event after event across the point's batches. The
+    first two batches and the last one of each point, FP64."""
+    cfgs, starts = tp.scan_points(cfg_sqrts1000, 256, 12345)
+    pick = [0, 1, 137]
+    sub = [cfgs[p] for p in pick]
+    with tp.Context(0) as ctx:
+        parts = ctx.run_points(sub, starts[pick], 0)
+    for p, cfg, part in zip(pick, sub, parts):
+        nb = cfg.num_batches
+        assert part.n == nb
+        got = part.as_array()
+        for b0, n in ((0, 2), (nb - 1, 1)):
+            ref = oracle.run_batches_jumped(cfg, b0, n, tp.rng_flags("xoshiro"), tp.XOSHIRO_DEFAULT_SEED, p).as_array()
+            a = got[b0:b0 + n]
+            assert np.array_equal(a[:, 0], ref[:, 0]), (p, b0)
+            scale = np.maximum(np.abs(ref[:, 1:]), np.abs(ref[:, 1:2]))
+            assert np.all(np.abs(a[:, 1:] - ref[:, 1:]) <= 1e-12 * np.maximum(scale, 1e-300)), (p, b0)

@@ -90,3 +90,15 @@ def test_ranf_noncanonical_seed_rejected(tp, oracle):
     assert tp.library().tp_ranf_state_at(1_000_000_970, 100, slots, ctypes.byref(index)) == tp.TP_ERR_UNSUPPORTED
     st = oracle.ranf_state(1_000_000_970, 0)[:55]
     assert any(v < 0 or v >= 10**9 for v in st)
+
+
+def test_jumped_stream_is_per_batch_stream(tp, oracle, cfg_valeurs):
+    """The restatement's stream of scan point p (seed jumped p times) starts
+    where batch p of the per-batch-jump mode starts, for both generators."""
+    cfg = cfg_valeurs.replace(num_events=60_000)
+    for rng in ("xoshiro", "ranf"):
+        kind, seed = tp.rng_flags(rng), tp.default_seed(rng)
+        for p in (1, 4):
+            a = oracle.run_batches_jumped(cfg, 0, 1, kind, seed, p, threads=1).as_array()
+            b = oracle.run_batches(cfg, p, 1, tp.rng_flags(rng, jump_per_batch=True), seed, threads=1).as_array()
+            assert np.array_equal(a, b), (rng, p)

@@ -1,8 +1,8 @@
 """tp_run_batches_noalloc, the entry point for callers that cannot allocate
-GPU memory (graph capture in progress, start-up-planned memory, a foreign
-allocator): called through the C ABI on the current device with output
-arrays the test owns, twice in a row, against the regular entry point
-tp_run_batches on the same batches. The library's fixed working memory is
+GPU memory (memory planned once at start-up, a foreign allocator that owns
+the GPU's memory): called through the C ABI on the current device with
+output arrays the test owns, twice in a row, against the regular entry
+point tp_run_batches on the same batches. The library's fixed working memory is
 shared by both calls; the second call must not see the first one's data.
 
 This file is collected last so that a run stopping at the first failure has
@@ -66,6 +66,11 @@ def test_noalloc_matches_regular_entry_point_twice(tp, cfg_valeurs, precision):
     assert_same(second, ref_b)
     again = call_noalloc(tp, torch, cfg, 17, 40, precision)
     assert_same(again, ref_a)
+    # the other accepted flag: photons left in generation order
+    with tp.Context(0) as ctx:
+        ref_c = ctx.run_batches(cfg, 3, 5, rng="xoshiro", precision=precision, sorting=False)
+    unsorted = call_noalloc(tp, torch, cfg, 3, 5, precision, tp.TP_MODE_NO_PHOTON_SORTING)
+    assert_same(unsorted, ref_c)
 
 
 def test_noalloc_rejects_oversized_ranges(tp, cfg_valeurs):
