@@ -156,10 +156,10 @@ def cpu_baseline(tp, events_budget_s=3.0):
 
 # DFMA-equivalent cost of CUDA 13.0's own FP64 log, sincos, sqrt and
 # division on GB300, measured once (8 independent chains per thread at full
-# occupancy against 16-chain DFMA, the method of tp_probe_fp64) and frozen
-# here, so that a cheaper implementation in the kernel raises frac_fixed
-# instead of lowering the work it is credited with.
-FROZEN_LIBM_COST = {"log": None, "sincos": 24.9, "sqrt": 8.6, "div": 8.6}
+# occupancy against 16-chain DFMA, the method of tp_probe_fp64; DFMA rate
+# 1.058e12 flop/s) and frozen here, so that a cheaper implementation in the
+# kernel raises frac_fixed instead of lowering the work it is credited with.
+FROZEN_LIBM_COST = {"log": 30.23, "sincos": 24.94, "sqrt": 8.62, "div": 8.61}
 
 
 def fixed_fp64_fraction(torch, dev, f_acc, kernel_events_per_s, clocks):
@@ -384,29 +384,32 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
 def gradient_checks(tp, model, theta, h_rel=1e-4):
     """The adjoint gradient at `theta` (all four components non-zero away
     from beta+- = 0) against (1) the analytic gradient of the forward pass's
-    per-bin raw sums and (2) central differences (h = 1e-4 max(|theta_i|, 1))
-    of ln L evaluated from the same forward pass's per-bin sums, so both
-    references see the same events. Relative deviations per component."""
+    per-bin raw sums and (2) finite differences of ln L evaluated from the
+    same forward pass's per-bin sums, so both references see the same
+    events: the five-point stencil (8 D(h) - D(2h)) / 12 h with D(h) = ln
+    L(theta + h) - ln L(theta - h) summed bin by bin as (mu+ - mu-)(mu+ +
+    mu- - 2 d) / v, which avoids the cancellation of two large ln L values;
+    h = 1e-4 max(|theta_i|, 1). Relative deviations per component."""
     theta = np.array(theta, np.float64)
     _, grad, _, dsigma = model.gradient(theta)
     hist = model.last_hist
     ga, dsa = model.analytic_gradient(theta, hist)
 
-    def lnl(t):
-        mu = model._mu(hist, model.theta_cfg(t))[0]
-        return -0.5 * float(np.sum((mu - model.data) ** 2 / model.var))
+    def dlnl(tp_, tm):
+        a = model._mu(hist, model.theta_cfg(tp_))[0]
+        b = model._mu(hist, model.theta_cfg(tm))[0]
+        return -0.5 * float(np.sum((a - b) * (a + b - 2.0 * model.data) / model.var))
 
     fd = np.zeros(4)
     for i in range(4):
-        h = h_rel * max(abs(theta[i]), 1.0)
-        tp_, tm = theta.copy(), theta.copy()
-        tp_[i] += h
-        tm[i] -= h
-        fd[i] = (lnl(tp_) - lnl(tm)) / (2 * h)
+        e = np.zeros(4)
+        e[i] = h_rel * max(abs(theta[i]), 1.0)
+        fd[i] = (8.0 * dlnl(theta + e, theta - e) - dlnl(theta + 2 * e, theta - 2 * e)) / (12.0 * e[i])
     rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))
     return {"theta": theta.tolist(), "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": dsigma.tolist(),
             "max_rel_dev_vs_analytic": rel(grad, ga), "max_rel_dev_dsigma_vs_analytic": rel(dsigma, dsa),
-            "max_rel_dev_vs_central_diff": rel(grad, fd), "central_diff_h_rel": h_rel}
+            "max_rel_dev_vs_central_diff": rel(grad, fd), "central_diff": "five-point, h = %g max(|theta_i|, 1)"
+                                                                         % h_rel}
 
 
 def grad_leg(tp, ctx, args, events, fit_steps=200):
@@ -446,6 +449,11 @@ def grad_leg(tp, ctx, args, events, fit_steps=200):
            "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": (flux * s @ dk).tolist(),
            "max_rel_dev_vs_analytic": float(np.max(np.abs(grad - ga)) / np.max(np.abs(ga)))}
     out["at_test_point"] = gradient_checks(tp, model, (0.25, -0.1, 91.187, 2.49))
+    # the FP32-mixed bins against an FP64 forward pass over the same events:
+    # events that changed bin (certified binning: none)
+    h64 = ctx.binned_forward(model.theta_cfg(theta), 0, nb, bins, SEED, tp.TP_PREC_FP64)
+    h32 = model.last_hist
+    out["flipped_bins"] = int(np.abs(h32[:, 5] - h64[:, 5]).sum() // 2)
     if fit_steps:
         # recover beta+- from the pseudo-data: natural-gradient steps, each a
         # forward and an adjoint pass over all events. Only beta-^2 enters the

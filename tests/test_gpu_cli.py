@@ -30,13 +30,13 @@ def test_tp_run_reproduces_golden(tmp_path, record_property, features, args):
     res = (tmp_path / "res.data").read_text()
     assert res.splitlines()[1] == golden("res.data", features).splitlines()[1]
     assert compare(res, golden("res.data", features), rel_tol=1e-12) == []
-    # beyond the numeric comparison: how many printed fields (14 and 8
-    # significant digits) differ from the golden's text at all
+    # beyond the numeric comparison: the printed fields (14 and 8
+    # significant digits) equal the golden's text byte for byte
     n_res, n_out = differing_fields(res, golden("res.data", features)), differing_fields(out, golden("stdout.log",
                                                                                                      features))
     record_property("res_data_fields_differing", n_res)
     record_property("stdout_fields_differing", n_out)
-    print("features=%r: res.data fields differing from the golden text: %d, stdout: %d" % (features, n_res, n_out))
+    assert n_res == 0 and n_out == 0, (n_res, n_out)
     assert (tmp_path / "res.times").read_text().count("\n") == 6
     assert len((tmp_path / "pil.mc").read_text().splitlines()) == 2
 
