@@ -509,34 +509,34 @@ class Context:
         return out
 
     def binned_forward(self, cfg, first_batch, n_batches, binning, seed=XOSHIRO_DEFAULT_SEED,
-                       precision=TP_PREC_FP64, jump_per_batch=False):
+                       precision=TP_PREC_FP64, jump_per_batch=False, rng="xoshiro"):
         """Per-bin sums [n_bins, 8]: raw R_0..R_4, events, sum w, sum w^2."""
         nb = binning.n_emax * binning.n_cos
         out = np.zeros((nb, BIN_STRIDE), np.float64)
-        self.check(library().tp_binned_forward(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch),
+        self.check(library().tp_binned_forward(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch),
                                                seed, first_batch, n_batches, precision, ctypes.byref(binning),
                                                ctypes.c_void_p(out.ctypes.data)))
         return out
 
     def binned_adjoint(self, cfg, first_batch, n_batches, binning, bin_weight, seed=XOSHIRO_DEFAULT_SEED,
-                       precision=TP_PREC_FP64, jump_per_batch=False):
+                       precision=TP_PREC_FP64, jump_per_batch=False, rng="xoshiro"):
         """(g, s): g_c = sum_e r[bin(e)] raw_c,e, s_c = sum_e raw_c,e."""
         w = np.ascontiguousarray(bin_weight, np.float64)
         g = (ctypes.c_double * 5)()
         sm = (ctypes.c_double * 5)()
-        self.check(library().tp_binned_adjoint(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch),
+        self.check(library().tp_binned_adjoint(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch),
                                                seed, first_batch, n_batches, precision, ctypes.byref(binning),
                                                ctypes.c_void_p(w.ctypes.data), g, sm))
         return np.array(g[:]), np.array(sm[:])
 
     def grad(self, cfg, first_batch, n_batches, binning, bin_weight, seed=XOSHIRO_DEFAULT_SEED,
-             precision=TP_PREC_FP64, jump_per_batch=False):
+             precision=TP_PREC_FP64, jump_per_batch=False, rng="xoshiro"):
         """tp_grad: (d lnL/dtheta, d sigma/dtheta) for theta = (beta+, beta-,
         M_Z, Gamma_Z), r = bin_weight = d lnL / d mu per bin."""
         w = np.ascontiguousarray(bin_weight, np.float64)
         dl = (ctypes.c_double * 4)()
         ds = (ctypes.c_double * 4)()
-        self.check(library().tp_grad(self.h, ctypes.byref(cfg.c), rng_flags("xoshiro", jump_per_batch), seed,
+        self.check(library().tp_grad(self.h, ctypes.byref(cfg.c), rng_flags(rng, jump_per_batch), seed,
                                      first_batch, n_batches, precision, ctypes.byref(binning),
                                      ctypes.c_void_p(w.ctypes.data), dl, ds))
         return np.array(dl[:]), np.array(ds[:])
@@ -583,9 +583,9 @@ class BinnedGaussianLikelihood:
     for the adjoint.
     """
 
-    def __init__(self, ctx, cfg, seed, n_batches, data_hist, data_cfg, bins, precision=TP_PREC_FP64):
+    def __init__(self, ctx, cfg, seed, n_batches, data_hist, data_cfg, bins, precision=TP_PREC_FP64, rng="xoshiro"):
         self.ctx, self.cfg, self.seed, self.n_batches = ctx, cfg, seed, n_batches
-        self.bins, self.precision = bins, precision
+        self.bins, self.precision, self.rng = bins, precision, rng
         _, _, flux_d = coupling_factors(data_cfg)
         self.data = flux_d * data_hist[:, 6]
         var = flux_d ** 2 * data_hist[:, 7]
@@ -601,7 +601,7 @@ class BinnedGaussianLikelihood:
 
     def value(self, theta):
         cfg = self.theta_cfg(theta)
-        hist = self.ctx.binned_forward(cfg, 0, self.n_batches, self.bins, self.seed, self.precision)
+        hist = self.ctx.binned_forward(cfg, 0, self.n_batches, self.bins, self.seed, self.precision, rng=self.rng)
         self.last_hist = hist
         mu, k, _, flux = self._mu(hist, cfg)
         lnl = -0.5 * float(np.sum((mu - self.data) ** 2 / self.var))
@@ -612,7 +612,7 @@ class BinnedGaussianLikelihood:
         lnl, sigma, mu = self.value(theta)
         cfg = self.theta_cfg(theta)
         r = -(mu - self.data) / self.var
-        g, s = self.ctx.binned_adjoint(cfg, 0, self.n_batches, self.bins, r, self.seed, self.precision)
+        g, s = self.ctx.binned_adjoint(cfg, 0, self.n_batches, self.bins, r, self.seed, self.precision, rng=self.rng)
         _, dk, flux = coupling_factors(cfg)
         return lnl, flux * g @ dk, sigma, flux * s @ dk
 

@@ -317,8 +317,6 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     kp.hist = c->d_hist;
     kp.adj = c->d_adj;
   }
-  if (pass != Pass::kBatches && kind != TP_RNG_XOSHIRO256P)
-    return c->fail(TP_ERR_UNSUPPORTED, "binned and adjoint passes use the xoshiro256+ stream");
   uint64_t start[4];
   xoshiro_seed(seed, start);
   for (uint64_t c0 = 0; c0 < n_batches; c0 += kChunk) {
@@ -355,9 +353,9 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
     if (pass == Pass::kBatches)
       st = launch_events(rng_kind, kp, tpb, stream);
     else if (pass == Pass::kBinned)
-      st = launch_binned(kp, tpb, 0, stream);
+      st = launch_binned(rng_kind, kp, tpb, 0, stream);
     else
-      st = launch_adjoint(kp, tpb, stream);
+      st = launch_adjoint(rng_kind, kp, tpb, stream);
     if (e1) {
       cudaEventRecord(e1, stream);
       c->prof_marks.push_back({1, {e0, e1}});

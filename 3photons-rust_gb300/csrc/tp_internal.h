@@ -189,7 +189,7 @@ int launch_dump(int rng_kind, int precision, const EvConst& k, const uint64_t st
 // message returned by tp_last_error(NULL) on this thread
 void set_thread_error(const char* msg);
 int launch_probe(int op, int iters, int blocks, int tpb, double* d_sink, void* stream);
-int launch_binned(const KParams& p, int tpb, int grid, void* stream);
+int launch_binned(int rng_kind, const KParams& p, int tpb, int grid, void* stream);
 int launch_points(const PointsParams& p, int tpb, void* stream);
 // Four-Russians tables of a thread's xoshiro jump J(T): for each group g of
 // 4 state bits (64 groups) and each value v of the group, the XOR of the
@@ -198,7 +198,7 @@ constexpr int kJumpTabWords = 64 * 16 * 4;
 int launch_build_jump_tab(const uint64_t* d_poly, int n_threads, uint64_t* d_tab, void* stream);
 int points_grid(int precision, int occupancy, int tpb);  // persistent grid size on the current device
 int events_wave(int precision, int occupancy, int tpb);  // resident xoshiro event CTAs on the current device
-int launch_adjoint(const KParams& p, int tpb, void* stream);
+int launch_adjoint(int rng_kind, const KParams& p, int tpb, void* stream);
 // faster-evgen passes: chunk start states, chunk maps, thread start states,
 // events (batch_state = the thread start states)
 int launch_fe_seed(const FeParams& p, void* stream);

@@ -388,17 +388,22 @@ def gradient_checks(tp, model, theta, h_rel=1e-4):
     same forward pass's per-bin sums, so both references see the same
     events: the five-point stencil (8 D(h) - D(2h)) / 12 h with D(h) = ln
     L(theta + h) - ln L(theta - h) summed bin by bin as (mu+ - mu-)(mu+ +
-    mu- - 2 d) / v, which avoids the cancellation of two large ln L values;
-    h = 1e-4 max(|theta_i|, 1). Relative deviations per component."""
+    mu- - 2 d) / v and mu+ - mu- = flux R (K+ - K-), which avoids the
+    cancellation of two large ln L values (or mu values: the A term, most
+    of mu, does not depend on M_Z or Gamma_Z); h = 1e-4 max(|theta_i|, 1).
+    Relative deviations per component."""
     theta = np.array(theta, np.float64)
     _, grad, _, dsigma = model.gradient(theta)
     hist = model.last_hist
     ga, dsa = model.analytic_gradient(theta, hist)
 
     def dlnl(tp_, tm):
-        a = model._mu(hist, model.theta_cfg(tp_))[0]
-        b = model._mu(hist, model.theta_cfg(tm))[0]
-        return -0.5 * float(np.sum((a - b) * (a + b - 2.0 * model.data) / model.var))
+        a, kp, _, flux = model._mu(hist, model.theta_cfg(tp_))
+        b, km, _, _ = model._mu(hist, model.theta_cfg(tm))
+        # mu+ - mu- from the difference of the coupling factors: the terms
+        # that do not depend on theta_i cancel exactly
+        dmu = flux * hist[:, :5] @ (kp - km)
+        return -0.5 * float(np.sum(dmu * (a + b - 2.0 * model.data) / model.var))
 
     fd = np.zeros(4)
     for i in range(4):

@@ -262,7 +262,12 @@ int tp_autotune(tp_ctx *ctx, const tp_config *cfg, int precision,
  * src/resacc.rs:59-100), on theta = (beta+, beta-, M_Z, Gamma_Z). Bins:
  * x = energy of the most energetic photon, y = cosine of its angle to the
  * electron beam; bin index ix * n_cos + iy; values outside the range go to
- * the edge bins. Both passes use the xoshiro256+ stream. */
+ * the edge bins. Both passes take either stream (rng_kind as for
+ * tp_run_batches, TP_MODE_FASTER_EVGEN excepted). TP_PREC_FP32_MIXED bins
+ * in FP32 with a certified decision: an event whose FP32 leading-photon
+ * energy or cosine lies within its error bound of an inner bin edge is
+ * binned from FP64 momenta, so every event lands in the bin of the FP64
+ * pass (its sums carry FP32 rounding). */
 typedef struct tp_binning {
   int32_t n_emax, n_cos;    /* n_emax * n_cos <= 1024                       */
   double emax_lo, emax_hi;  /* GeV; both 0: [sqrt(s)/3, sqrt(s)/2]           */

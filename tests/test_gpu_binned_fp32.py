@@ -23,10 +23,11 @@ def test_fp32_bins_equal_fp64_bins(tp, ctx, cfg_sqrts1000, seed, betas):
     # sum wherever a bin holds 1000 events or more (single events carry FP32
     # errors up to 1e-4 in their B+- sums, which sparse edge bins do not
     # average away: 1e-4 there); the interference sums, which cancel, on
-    # the scale of the bin's A sum
+    # their natural scale sqrt(|A| |B+|) in the bin
     full = h64[:, 5] >= 1000
+    natural = np.sqrt(np.abs(h64[:, 0] * h64[:, 1]))
     for c in range(8):
-        scale = np.abs(h64[:, c]) if c not in (3, 4) else np.maximum(np.abs(h64[:, c]), np.abs(h64[:, 0]))
+        scale = np.abs(h64[:, c]) if c not in (3, 4) else np.maximum(np.abs(h64[:, c]), natural)
         rel = np.abs(h32[:, c] - h64[:, c]) / np.maximum(scale, 1e-300)
         print("sum %d: max rel. error %.2e over full bins, %.2e over all" % (c, rel[full].max(), rel.max()))
         assert rel[full].max() <= 1e-6 and rel.max() <= 1e-4, c
