@@ -175,6 +175,8 @@ def library():
         "tp_run_batches_noalloc": (i32, [P(CConfig), i32, u64, u64, u64, i32, P(CBatchSoa), vp]),
         "tp_run_points": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_uint64), i32, i32,
                                 P(ctypes.c_uint64), P(CBatchSoa), u64]),
+        "tp_run_points_ranf": (i32, [vp, ctypes.c_uint32, P(CConfig), P(ctypes.c_int32), i32, i32,
+                                     P(ctypes.c_uint64), P(CBatchSoa), u64]),
         "tp_autotune": (i32, [vp, P(CConfig), i32, u64, P(ctypes.c_int), P(ctypes.c_double)]),
         "tp_binned_forward": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp]),
         "tp_binned_adjoint": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, P(CBinning), vp,
@@ -481,21 +483,26 @@ class Context:
                                          ctypes.byref(rate)))
         return ept.value, rate.value
 
-    def run_points(self, cfgs, starts, precision=TP_PREC_FP32_MIXED, sorting=True):
+    def run_points(self, cfgs, starts, precision=TP_PREC_FP32_MIXED, sorting=True, rng="xoshiro"):
         """Batched form: every point's run in one persistent launch (CUDA
-        graph). starts: [n_points, 4] raw xoshiro states. Returns one
-        BatchAccumulators per point."""
+        graph). starts: [n_points, 4] raw xoshiro states, or (rng="ranf")
+        [n_points] ranf seeds. Returns one BatchAccumulators per point."""
         n = len(cfgs)
         arr = (CConfig * n)(*[c.c for c in cfgs])
-        st = np.ascontiguousarray(starts, np.uint64).reshape(n, 4)
         total = sum((c.num_events + TP_BATCH_SIZE - 1) // TP_BATCH_SIZE for c in cfgs)
         acc = BatchAccumulators(total)
         unit0 = np.zeros(n + 1, np.uint64)
         soa = acc.soa()
-        self.check(library().tp_run_points(self.h, n, arr, st.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
-                                           0 if sorting else TP_MODE_NO_PHOTON_SORTING, precision,
-                                           unit0.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.byref(soa),
-                                           total))
+        flags = 0 if sorting else TP_MODE_NO_PHOTON_SORTING
+        u0 = unit0.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        if rng == "ranf":
+            st = np.ascontiguousarray(starts, np.int32).reshape(n)
+            self.check(library().tp_run_points_ranf(self.h, n, arr, st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                    flags, precision, u0, ctypes.byref(soa), total))
+        else:
+            st = np.ascontiguousarray(starts, np.uint64).reshape(n, 4)
+            self.check(library().tp_run_points(self.h, n, arr, st.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                               flags, precision, u0, ctypes.byref(soa), total))
         out = []
         for p in range(n):
             a, b = int(unit0[p]), int(unit0[p + 1])
@@ -632,12 +639,14 @@ def xoshiro_start(seed, jumps128=0, draws=0):
     return list(s)
 
 
-def scan_points(base, n_points=256, seed=12345):
+def scan_points(base, n_points=256, seed=12345, rng="xoshiro"):
     """Parameter points of the batched form: sqrt(s) ~ U[200, 2000] GeV,
     E_min ~ U[1, 50] GeV, the |cos| cuts (beam-photon and photon-photon) ~
     U[0.80, 0.99], beta+, beta- ~ U[-1, 1], events ~ log-U[1e6, 1e8], drawn
     with numpy's PCG64(seed); everything else from `base`. Point p's stream
-    is xoshiro256+ seeded with 12345 and jumped p times by 2^128."""
+    is the reference's stream jumped p times (RandomGenerator::jump):
+    xoshiro256+ seeded with 12345 and jumped p times by 2^128 (starts: raw
+    states), or ranf seeded with 234612947 + 123456 p (starts: the seeds)."""
     r = np.random.Generator(np.random.PCG64(seed))
     cfgs, starts = [], []
     for p in range(n_points):
@@ -646,8 +655,11 @@ def scan_points(base, n_points=256, seed=12345):
                                  beam_photons_cut=cut, photon_photon_cut=cut,
                                  beta_plus=float(r.uniform(-1.0, 1.0)), beta_minus=float(r.uniform(-1.0, 1.0)),
                                  num_events=int(np.exp(r.uniform(np.log(1e6), np.log(1e8))))))
-        starts.append(xoshiro_start(XOSHIRO_DEFAULT_SEED, p))
-    return cfgs, np.array(starts, np.uint64)
+        if rng == "ranf":
+            starts.append(np.int32(np.uint32((RANF_DEFAULT_SEED + 123456 * p) & 0xffffffff).view(np.int32)))
+        else:
+            starts.append(xoshiro_start(XOSHIRO_DEFAULT_SEED, p))
+    return cfgs, np.array(starts, np.int32 if rng == "ranf" else np.uint64)
 
 
 def fisher_matrix(model, theta, hist=None):

@@ -133,7 +133,7 @@ struct tp_ctx {
     size_t bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    uint64_t key[7] = {0, 0, 0, 0, 0, 0, 0};  // n_points, n_units, precision, ept, flags, buffer, variant
+    uint64_t key[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // n_points, n_units, precision, ept, flags, buffer, variant, kind
   } pts;
   // optional CUDA-event timing of every kernel launch (tp_profile)
   int prof = 0;
@@ -849,8 +849,12 @@ int tp_grad(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64
   return TP_OK;
 }
 
-int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uint64_t* starts, int mode_flags,
-                  int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
+namespace {
+
+// tp_run_points and tp_run_points_ranf: `starts` holds xoshiro states
+// (4 x u64 per point) or ranf seeds (one i32 per point).
+int run_points(tp_ctx* c, int kind, uint32_t n_points, const tp_config* cfgs, const void* starts, int mode_flags,
+               int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
   if (!c) return TP_ERR_INVALID;
   if (!cfgs || !starts || !unit0 || !out || !out->selected || !out->spm2 || !out->vars || !out->sigma ||
       !out->variance)
@@ -877,12 +881,33 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   for (uint32_t p = 0; p < n_points; ++p)
     for (uint64_t u = unit0[p]; u < unit0[p + 1]; ++u) unit_point[u] = p;
   const int pi = prec_index(precision);
-  if (int st = ensure_thread_poly(c, pi)) return st;
+  const bool ranf = kind == TP_RNG_RANF;
+  // ranf: each point's stream from its seed (blocks 0 and 1, the window
+  // every batch start is jumped from)
+  std::vector<int32_t> windows;
+  if (ranf) {
+    if (int st = ensure_ranf_blocks(c)) return st;
+    windows.resize(110 * (size_t)n_points);
+    const int32_t* seeds = static_cast<const int32_t*>(starts);
+    for (uint32_t p = 0; p < n_points; ++p) {
+      int32_t* w = windows.data() + 110 * (size_t)p;
+      ranf_seeded(seeds[p], w);
+      if (!ranf_canonical(w))
+        return c->fail(TP_ERR_UNSUPPORTED, "ranf seed of point " + std::to_string(p) +
+                                               " gives a state outside [0, 1e9): no jump-ahead");
+      for (int i = 0; i < 55; ++i) w[55 + i] = w[i];
+      ranf_reset(w + 55);
+    }
+  } else if (int st = ensure_thread_poly(c, pi)) {
+    return st;
+  }
   // one device buffer, 256-byte aligned sections
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t start_bytes = ranf ? n_points * 110 * sizeof(int32_t) : n_points * 32;
+  const size_t state_bytes = ranf ? 56 * sizeof(int32_t) : 32;
   const size_t o_pts = 0, o_ev = o_pts + al(n_points * sizeof(EvConst)), o_u0 = o_ev + al(n_points * 8),
-               o_st = o_u0 + al(n_points * 8), o_up = o_st + al(n_points * 32), o_us = o_up + al(n_units * 4),
-               o_out = o_us + al(n_units * 32), o_cnt = o_out + al(n_units * 13 * 8), total = o_cnt + 256;
+               o_st = o_u0 + al(n_points * 8), o_up = o_st + al(start_bytes), o_us = o_up + al(n_units * 4),
+               o_out = o_us + al(n_units * state_bytes), o_cnt = o_out + al(n_units * 13 * 8), total = o_cnt + 256;
   if (c->pts.bytes < total) {
     if (c->pts.buf) cudaFree(c->pts.buf);
     c->pts.buf = nullptr;
@@ -892,13 +917,17 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   }
   char* base = static_cast<char*>(c->pts.buf);
   PointsParams pp{};
+  pp.kind = kind;
   pp.points = reinterpret_cast<const EvConst*>(base + o_pts);
   pp.point_events = reinterpret_cast<const uint64_t*>(base + o_ev);
   pp.point_unit0 = reinterpret_cast<const uint64_t*>(base + o_u0);
   pp.point_start = reinterpret_cast<const uint64_t*>(base + o_st);
+  pp.point_window = reinterpret_cast<const int32_t*>(base + o_st);
   pp.unit_point = reinterpret_cast<const uint32_t*>(base + o_up);
-  pp.unit_state = reinterpret_cast<uint64_t*>(base + o_us);
+  pp.unit_state = base + o_us;
   pp.batch_table = c->d_xo_batch;
+  pp.ranf_table = c->d_ranf_tab;
+  pp.ranf_blocks = c->d_ranf_blocks;
   pp.thread_poly = c->d_thread_poly[pi];
   pp.jump_tab = c->d_jump_tab[pi];
   pp.counter = reinterpret_cast<unsigned long long*>(base + o_cnt);
@@ -917,12 +946,12 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   up(o_pts, pk.data(), n_points * sizeof(EvConst));
   up(o_ev, pev.data(), n_points * 8);
   up(o_u0, unit0, n_points * 8);
-  up(o_st, starts, n_points * 32);
+  up(o_st, ranf ? (const void*)windows.data() : starts, start_bytes);
   up(o_up, unit_point.data(), n_units * 4);
   if (st) return st;
   // the seeding + persistent launches are captured once per shape and replayed
-  const uint64_t key[7] = {n_points, n_units, (uint64_t)precision, (uint64_t)pp.ept, (uint64_t)mode_flags,
-                           (uint64_t)(uintptr_t)c->pts.buf, (uint64_t)pp.occupancy};
+  const uint64_t key[8] = {n_points, n_units, (uint64_t)precision, (uint64_t)pp.ept, (uint64_t)mode_flags,
+                           (uint64_t)(uintptr_t)c->pts.buf, (uint64_t)pp.occupancy, (uint64_t)kind};
   if (!c->pts.exec || std::memcmp(key, c->pts.key, sizeof key) != 0) {
     if (c->pts.exec) cudaGraphExecDestroy(c->pts.exec);
     if (c->pts.graph) cudaGraphDestroy(c->pts.graph);
@@ -968,6 +997,18 @@ int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uin
   if (!st) st = c->cuda(cudaMemcpyAsync(out->variance, pp.out.variance, n * 8, cudaMemcpyDeviceToHost, c->stream), "copy results");
   if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "run points");
   return st;
+}
+
+}  // namespace
+
+int tp_run_points(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const uint64_t* starts, int mode_flags,
+                  int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
+  return run_points(c, TP_RNG_XOSHIRO256P, n_points, cfgs, starts, mode_flags, precision, unit0, out, capacity);
+}
+
+int tp_run_points_ranf(tp_ctx* c, uint32_t n_points, const tp_config* cfgs, const int32_t* seeds, int mode_flags,
+                       int precision, uint64_t* unit0, tp_batch_soa* out, uint64_t capacity) {
+  return run_points(c, TP_RNG_RANF, n_points, cfgs, seeds, mode_flags, precision, unit0, out, capacity);
 }
 
 int tp_autotune(tp_ctx* c, const tp_config* cfg, int precision, uint64_t sample_batches, int* best_ept,

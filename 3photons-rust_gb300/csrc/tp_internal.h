@@ -87,15 +87,19 @@ struct KParams {
 // Batched form: many parameter points in one persistent launch. Work unit
 // u = one 10k batch of one point; units are numbered point by point.
 struct PointsParams {
+  int kind;                         // TP_RNG_XOSHIRO256P or TP_RNG_RANF
   const EvConst* points;            // [n_points]
   const uint64_t* point_events;     // [n_points] events of each point's run
   const uint64_t* point_unit0;      // [n_points] first unit of each point
-  const uint64_t* point_start;      // [n_points][4] xoshiro state at draw 0
+  const uint64_t* point_start;      // xoshiro: [n_points][4] state at draw 0
+  const int32_t* point_window;      // ranf: [n_points][110] blocks 0 and 1 of the point's stream
   const uint32_t* unit_point;       // [n_units]
-  const uint64_t* batch_table;      // 64 x 4: x^(12e4 * 2^k)
-  const uint64_t* thread_poly;      // x^(12 ept j)
-  const uint64_t* jump_tab;         // the same as tables, or null
-  uint64_t* unit_state;             // [n_units][4] scratch: batch start states
+  const uint64_t* batch_table;      // xoshiro: 64 x 4: x^(12e4 * 2^k)
+  const uint64_t* thread_poly;      // xoshiro: x^(12 ept j)
+  const uint64_t* jump_tab;         // xoshiro: the same as tables, or null
+  const uint32_t* ranf_table;       // ranf: x^(55 2^k) mod P
+  const uint32_t* ranf_blocks;      // ranf: x^(55 D) mod P for D < kRanfBlocksInBatch
+  void* unit_state;                 // [n_units] scratch: batch start states (xoshiro 4 x u64, ranf 56 x i32)
   unsigned long long* counter;      // work-queue head, 0 at launch
   unsigned long long* recheck_count;
   BatchOut out;                     // stride n_units

@@ -240,6 +240,17 @@ int tp_run_points(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
                   const uint64_t *starts, int mode_flags, int precision,
                   uint64_t *unit0, tp_batch_soa *out, uint64_t capacity);
 
+/* tp_run_points on the ranf stream (the reference's default generator):
+ * point p's stream is RanfGenerator seeded with seeds[p] (seeded_new,
+ * src/random/ranf.rs:36-66), consumed 12 draws per event through the
+ * point's batches. A scan that gives point p the reference's p-th jump
+ * (RandomGenerator::jump, src/random/ranf.rs:137-140) passes
+ * seeds[p] = seed + 123456 p. A seed whose state leaves [0, 1e9) gives
+ * TP_ERR_UNSUPPORTED (no jump-ahead). Other arguments as tp_run_points. */
+int tp_run_points_ranf(tp_ctx *ctx, uint32_t n_points, const tp_config *cfgs,
+                       const int32_t *seeds, int mode_flags, int precision,
+                       uint64_t *unit0, tp_batch_soa *out, uint64_t capacity);
+
 /* Autotuner: times the xoshiro event kernel of `precision` on the first
  * `sample_batches` batches of cfg for each candidate events-per-thread
  * (which fixes the block shape, ceil(10000 / ept) threads rounded to

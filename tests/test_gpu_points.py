@@ -84,3 +84,44 @@ def test_scan_points_match_restatement(tp, oracle, cfg_sqrts1000):
             assert np.array_equal(a[:, 0], ref[:, 0]), (p, b0)
             scale = np.maximum(np.abs(ref[:, 1:]), np.abs(ref[:, 1:2]))
             assert np.all(np.abs(a[:, 1:] - ref[:, 1:]) <= 1e-12 * np.maximum(scale, 1e-300)), (p, b0)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32-mixed"])
+def test_ranf_points_match_one_point_path(tp, cfg_valeurs, precision):
+    """The batched form on the reference's default stream: point p is ranf
+    seeded with its own seed, against tp_run_batches on that seed."""
+    cfgs, _, _ = small_points(tp, cfg_valeurs)
+    seeds = [tp.RANF_DEFAULT_SEED + 123456 * p for p in range(len(cfgs))]
+    with tp.Context(0) as ctx:
+        parts = ctx.run_points(cfgs, seeds, precision, rng="ranf")
+        again = ctx.run_points(cfgs, seeds, precision, rng="ranf")  # graph replay
+        for cfg, seed, part, rep in zip(cfgs, seeds, parts, again):
+            ref = ctx.run_batches(cfg, 0, cfg.num_batches, rng="ranf", seed=seed, precision=precision)
+            assert np.array_equal(part.selected, ref.selected)
+            a, b = part.as_array()[:, 1:], ref.as_array()[:, 1:]
+            # as for xoshiro: FP32 products may contract differently in the
+            # two kernels; the counts (certified cuts) stay exact
+            tol = 1e-12 if precision == 0 else 1e-5
+            scale = np.maximum(np.abs(b), np.abs(b[:, :1]))
+            assert np.all(np.abs(a - b) <= tol * np.maximum(scale, 1e-300))
+            assert rep.as_array().tobytes() == part.as_array().tobytes()
+
+
+def test_ranf_scan_points_match_restatement(tp, oracle, cfg_sqrts1000):
+    """Points of the ranf scan (point p seeded 234612947 + 123456 p, the
+    reference's p-th RandomGenerator::jump) against the CPU restatement of
+    the same point, FP64: first two batches and the last one."""
+    cfgs, seeds = tp.scan_points(cfg_sqrts1000, 256, 12345, rng="ranf")
+    pick = [0, 3, 200]
+    sub = [cfgs[p] for p in pick]
+    with tp.Context(0) as ctx:
+        parts = ctx.run_points(sub, seeds[pick], 0, rng="ranf")
+    for p, cfg, part in zip(pick, sub, parts):
+        nb = cfg.num_batches
+        got = part.as_array()
+        for b0, n in ((0, 2), (nb - 1, 1)):
+            ref = oracle.run_batches_jumped(cfg, b0, n, tp.rng_flags("ranf"), tp.RANF_DEFAULT_SEED, p).as_array()
+            a = got[b0:b0 + n]
+            assert np.array_equal(a[:, 0], ref[:, 0]), (p, b0)
+            scale = np.maximum(np.abs(ref[:, 1:]), np.abs(ref[:, 1:2]))
+            assert np.all(np.abs(a[:, 1:] - ref[:, 1:]) <= 1e-12 * np.maximum(scale, 1e-300)), (p, b0)
