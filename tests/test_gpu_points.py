@@ -7,6 +7,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+def batch_scale(b):
+    """Per-element scale of (n, 12) batch sums (spm2[5], vars[5], sigma,
+    variance): each sum's own size or its batch's A sum, and for the
+    interference sums (which cancel) their natural size sqrt(|A| |B+|)."""
+    scale = np.maximum(np.abs(b), np.abs(b[:, :1]))
+    natural = np.sqrt(np.abs(b[:, 0] * b[:, 1]))
+    scale[:, 3:5] = np.maximum(np.abs(b[:, 3:5]), natural[:, None])
+    return scale
+
+
 def small_points(tp, base, n=12, seed=5):
     cfgs, _ = tp.scan_points(base, n, seed)
     r = np.random.default_rng(seed)
@@ -33,8 +43,7 @@ def test_points_match_one_point_path(tp, cfg_valeurs, precision):
             for got in (part, rep):
                 assert np.array_equal(got.selected, ref.selected)
                 a, b = got.as_array()[:, 1:], ref.as_array()[:, 1:]
-                scale = np.maximum(np.abs(b), np.abs(b[:, :1]))
-                assert np.all(np.abs(a - b) <= tol * np.maximum(scale, 1e-300))
+                assert np.all(np.abs(a - b) <= tol * np.maximum(batch_scale(b), 1e-300))
             assert rep.as_array().tobytes() == part.as_array().tobytes()  # graph replay is deterministic
 
 
@@ -82,7 +91,7 @@ def test_scan_points_match_restatement(tp, oracle, cfg_sqrts1000):
             ref = oracle.run_batches_jumped(cfg, b0, n, tp.rng_flags("xoshiro"), tp.XOSHIRO_DEFAULT_SEED, p).as_array()
             a = got[b0:b0 + n]
             assert np.array_equal(a[:, 0], ref[:, 0]), (p, b0)
-            scale = np.maximum(np.abs(ref[:, 1:]), np.abs(ref[:, 1:2]))
+            scale = batch_scale(ref[:, 1:])
             assert np.all(np.abs(a[:, 1:] - ref[:, 1:]) <= 1e-12 * np.maximum(scale, 1e-300)), (p, b0)
 
 
@@ -102,8 +111,7 @@ def test_ranf_points_match_one_point_path(tp, cfg_valeurs, precision):
             # as for xoshiro: FP32 products may contract differently in the
             # two kernels; the counts (certified cuts) stay exact
             tol = 1e-12 if precision == 0 else 1e-5
-            scale = np.maximum(np.abs(b), np.abs(b[:, :1]))
-            assert np.all(np.abs(a - b) <= tol * np.maximum(scale, 1e-300))
+            assert np.all(np.abs(a - b) <= tol * np.maximum(batch_scale(b), 1e-300))
             assert rep.as_array().tobytes() == part.as_array().tobytes()
 
 
@@ -123,5 +131,5 @@ def test_ranf_scan_points_match_restatement(tp, oracle, cfg_sqrts1000):
             ref = oracle.run_batches_jumped(cfg, b0, n, tp.rng_flags("ranf"), tp.RANF_DEFAULT_SEED, p).as_array()
             a = got[b0:b0 + n]
             assert np.array_equal(a[:, 0], ref[:, 0]), (p, b0)
-            scale = np.maximum(np.abs(ref[:, 1:]), np.abs(ref[:, 1:2]))
+            scale = batch_scale(ref[:, 1:])
             assert np.all(np.abs(a[:, 1:] - ref[:, 1:]) <= 1e-12 * np.maximum(scale, 1e-300)), (p, b0)
