@@ -381,7 +381,7 @@ def fp32_leg(tp, ctx, torch, dev, stream, args, events, world, rank, fp64_value,
     return out
 
 
-def gradient_checks(tp, model, theta, h_rel=1e-4):
+def gradient_checks(tp, model, theta, h_rel=(1e-2, 1e-2, 1e-4, 1e-2)):
     """The adjoint gradient at `theta` (all four components non-zero away
     from beta+- = 0) against (1) the analytic gradient of the forward pass's
     per-bin raw sums and (2) finite differences of ln L evaluated from the
@@ -390,8 +390,12 @@ def gradient_checks(tp, model, theta, h_rel=1e-4):
     L(theta + h) - ln L(theta - h) summed bin by bin as (mu+ - mu-)(mu+ +
     mu- - 2 d) / v and mu+ - mu- = flux R (K+ - K-), which avoids the
     cancellation of two large ln L values (or mu values: the A term, most
-    of mu, does not depend on M_Z or Gamma_Z); h = 1e-4 max(|theta_i|, 1).
-    Relative deviations per component."""
+    of mu, does not depend on M_Z or Gamma_Z). Steps h_i = h_rel[i]
+    max(|theta_i|, 1): ln L is a polynomial in beta+- (any step is exact)
+    and at sqrt(s) = 1000 GeV mu depends on Gamma_Z only through
+    (Gamma_Z / M_Z)^2 next to (s / M_Z^2 - 1)^2 = 1.4e4, so a step of 1e-4
+    changes K by 1e-11 relative, below what its rounding resolves: 1e-2
+    there; 1e-4 for M_Z. Relative deviations per component."""
     theta = np.array(theta, np.float64)
     _, grad, _, dsigma = model.gradient(theta)
     hist = model.last_hist
@@ -408,13 +412,13 @@ def gradient_checks(tp, model, theta, h_rel=1e-4):
     fd = np.zeros(4)
     for i in range(4):
         e = np.zeros(4)
-        e[i] = h_rel * max(abs(theta[i]), 1.0)
+        e[i] = h_rel[i] * max(abs(theta[i]), 1.0)
         fd[i] = (8.0 * dlnl(theta + e, theta - e) - dlnl(theta + 2 * e, theta - 2 * e)) / (12.0 * e[i])
     rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))
     return {"theta": theta.tolist(), "dlnL_dtheta": grad.tolist(), "dsigma_dtheta": dsigma.tolist(),
             "max_rel_dev_vs_analytic": rel(grad, ga), "max_rel_dev_dsigma_vs_analytic": rel(dsigma, dsa),
-            "max_rel_dev_vs_central_diff": rel(grad, fd), "central_diff": "five-point, h = %g max(|theta_i|, 1)"
-                                                                         % h_rel}
+            "max_rel_dev_vs_central_diff": rel(grad, fd),
+            "central_diff": "five-point, h_i = %s max(|theta_i|, 1)" % list(h_rel)}
 
 
 def grad_leg(tp, ctx, args, events, fit_steps=200):
@@ -510,6 +514,38 @@ def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=
            "selected": int(sel.sum().item())}
     if fp64_value:
         out["vs_default_evgen_fp64"] = out["events_per_s"] / fp64_value
+    return out
+
+
+def ranf_leg(tp, ctx, torch, dev, stream, events, xoshiro_fp32_value):
+    """The reference's default stream (ranf, seed 234612947) on the same
+    physics, 1e9 events per step, FP64 and FP32-mixed, device-resident
+    outputs, CUDA events on the launching stream."""
+    cfg = workload_config(tp, events)
+    nb = (events + tp.TP_BATCH_SIZE - 1) // tp.TP_BATCH_SIZE
+    sel = torch.zeros(nb, dtype=torch.int64, device=dev)
+    f = torch.zeros(12 * nb, dtype=torch.float64, device=dev)
+    ptrs = [sel.data_ptr(), f.data_ptr(), f.data_ptr() + 5 * nb * 8, f.data_ptr() + 10 * nb * 8,
+            f.data_ptr() + 11 * nb * 8]
+    out = {"events": events}
+    for name, prec in (("fp64", tp.TP_PREC_FP64), ("fp32", tp.TP_PREC_FP32_MIXED)):
+        def step():
+            ctx.run_batches_device(cfg, 0, nb, ptrs, stream=stream.cuda_stream, rng="ranf",
+                                   seed=tp.RANF_DEFAULT_SEED, precision=prec)
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                step()
+        torch.cuda.synchronize()
+        steps = 3
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            for _ in range(steps):
+                step()
+            b.record(stream)
+        torch.cuda.synchronize()
+        out[name] = events * steps / (a.elapsed_time(b) * 1e-3)
+    out["fp32_over_xoshiro"] = out["fp32"] / xoshiro_fp32_value
     return out
 
 
@@ -764,6 +800,7 @@ def main():
     if world == 1:
         line["grad"] = grad_leg(tp, ctx, args, events)
         line["batched"] = points_leg(tp, ctx, args)
+        line["ranf"] = ranf_leg(tp, ctx, torch, dev, stream, events, fp32["value"])
         line["faster_evgen"] = [faster_evgen_leg(tp, ctx, torch, dev, stream, events, "xoshiro", SEED, value),
                                 faster_evgen_leg(tp, ctx, torch, dev, stream, events // 5, "ranf",
                                                  tp.RANF_DEFAULT_SEED)]
