@@ -329,7 +329,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
       st = launch_seed_xoshiro(start, jpb ? c->d_xo_jump : c->d_xo_batch, fb, cn,
                                static_cast<uint64_t*>(c->d_state), stream);
     else
-      st = launch_seed_ranf(jpb, (int32_t)seed, c->d_ranf_window, c->d_ranf_tab, fb, cn,
+      st = launch_seed_ranf(jpb, (int32_t)seed, c->d_ranf_window, c->d_ranf_tab, c->d_ranf_blocks, fb, cn,
                             static_cast<int32_t*>(c->d_state), stream);
     if (e1) {
       cudaEventRecord(e1, stream);

@@ -181,9 +181,9 @@ int check_config(const tp_config* cfg);
 // Kernel launchers (tp_kernels.cu); `stream` is a cudaStream_t
 int launch_seed_xoshiro(const uint64_t start[4], const uint64_t* d_table, uint64_t first_batch,
                         uint64_t n_batches, uint64_t* d_out, void* stream);
-int launch_seed_ranf(int jump_per_batch, int32_t seed, const int32_t* d_window,
-                     const uint32_t* d_table, uint64_t first_batch, uint64_t n_batches,
-                     int32_t* d_out, void* stream);
+int launch_seed_ranf(int jump_per_batch, int32_t seed, const int32_t* d_window, const uint32_t* d_table,
+                     const uint32_t* d_blocks, uint64_t first_batch, uint64_t n_batches, int32_t* d_out,
+                     void* stream);
 int launch_events(int rng_kind, const KParams& p, int tpb, void* stream);
 int launch_dump(int rng_kind, int precision, const EvConst& k, const uint64_t start[4], const int32_t* d_window,
                 int32_t seed, const uint64_t* d_xo_draw_table, const uint64_t* d_xo_jump_table,
