@@ -475,8 +475,6 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
 
 int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_t first_batch, uint64_t n_batches,
            int precision, const BatchOut& out, cudaStream_t stream) {
-  if (precision != TP_PREC_FP64)
-    return c->fail(TP_ERR_UNSUPPORTED, "TP_MODE_FASTER_EVGEN runs in FP64 only");
   const int kind = rng_kind & TP_RNG_KIND_MASK;
   const bool jpb = (rng_kind & TP_MODE_JUMP_PER_BATCH) != 0;
   const uint64_t n_total = cfg->num_events;
@@ -484,7 +482,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
   fp.kind = kind;
   fp.jpb = jpb;
   fp.err = c->d_err;
-  fp.ept = c->ept[0];  // FP64 only
+  fp.ept = c->ept[0];  // the FP64 shape, for both precisions (the thread starts depend on it)
   const int tpb = (((kBatch + fp.ept - 1) / fp.ept) + 31) / 32 * 32;
   fp.tpb = tpb;
   fp.num_events = n_total;
@@ -505,6 +503,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
   kp.num_events = n_total;
   kp.precision = precision;
   kp.err = c->d_err;
+  kp.recheck_count = c->d_recheck;
   kp.ept = fp.ept;
   const size_t state_bytes = kind == TP_RNG_RANF ? 56 * sizeof(int32_t) : 4 * sizeof(uint64_t);
   const uint64_t b_end = first_batch + n_batches;
@@ -1106,7 +1105,6 @@ int tp_fp32_error(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, 
                   uint64_t n_batches, double* err_vs_fp64, tp_batch_soa* fp32, tp_batch_soa* fp64) {
   if (!c) return TP_ERR_INVALID;
   if (!err_vs_fp64) return c->fail(TP_ERR_INVALID, "null output array");
-  if (rng_kind & TP_MODE_FASTER_EVGEN) return c->fail(TP_ERR_UNSUPPORTED, "TP_MODE_FASTER_EVGEN runs in FP64 only");
   if (n_batches == 0) return TP_OK;
   if (n_batches > (1ull << 32)) return c->fail(TP_ERR_INVALID, "batch range too large");
   const size_t n = n_batches;

@@ -80,7 +80,8 @@ extern "C" {
  * blocks, plus 2 per re-rolled unit-circle point, so the draws per event
  * vary. The library first finds every event's first draw (a pass over the
  * stream's accept bits from draw 0, also for first_batch > 0), then runs the
- * events. FP64 only (TP_PREC_FP32_MIXED gives TP_ERR_UNSUPPORTED), batch
+ * events, in FP64 or FP32-mixed (the same draws and accept decisions;
+ * FP32 physics with the certified cuts), batch
  * accumulators only (tp_run_batches / tp_run_batches_async); the _async call
  * waits for the boundary pass before it queues the event kernels. A
  * one-stream run keeps the pass's accept bits in device memory (about 5.8 GB
@@ -347,8 +348,8 @@ int tp_recheck_count(tp_ctx *ctx, uint64_t *count, int reset);
  * batch i's sums (spm2[5], vars[5], sigma, variance; the mixed terms on the
  * scale of the A sum), or -1 where the selected counts differ. Either run's
  * sums may be returned through the optional fp32 / fp64 arrays (NULL to
- * skip). No counterpart in the reference, which has no mixed-precision path;
- * TP_MODE_FASTER_EVGEN is FP64 only and gives TP_ERR_UNSUPPORTED. */
+ * skip). No counterpart in the reference, which has no mixed-precision
+ * path. */
 int tp_fp32_error(tp_ctx *ctx, const tp_config *cfg, int rng_kind,
                   uint64_t seed, uint64_t first_batch, uint64_t n_batches,
                   double *err_vs_fp64, tp_batch_soa *fp32, tp_batch_soa *fp64);

@@ -92,9 +92,6 @@ def test_deterministic(ctx, cfg_valeurs):
 
 def test_unsupported_combinations(tp, ctx, cfg_valeurs):
     cfg = cfg_valeurs.replace(num_events=10_000)
-    with pytest.raises(tp.TPError) as e:
-        ctx.run_batches(cfg, 0, 1, rng="xoshiro", precision=tp.TP_PREC_FP32_MIXED, faster_evgen=True)
-    assert e.value.code == tp.TP_ERR_UNSUPPORTED
     flags = tp.rng_flags("xoshiro", faster_evgen=True)
     bins = tp.binning(4, 4)
     hist = np.zeros((16, tp.BIN_STRIDE), np.float64)
@@ -120,3 +117,42 @@ def test_chunk_entered_past_the_mapped_offsets(tp, oracle, ctx, cfg_valeurs, see
     nb = cfg.num_batches
     gpu = ctx.run_batches(cfg, 0, nb, rng="xoshiro", seed=seed, faster_evgen=True)
     assert_batches_close(gpu, oracle_batches(tp, oracle, cfg, 0, nb, "xoshiro", False, True, seed))
+
+
+@pytest.mark.parametrize("rng,jump", [("xoshiro", False), ("ranf", False), ("xoshiro", True), ("ranf", True)])
+def test_fp32_mixed_selects_the_fp64_events(tp, ctx, cfg_sqrts1000, rng, jump):
+    """The precision form of faster-evgen (the reference's fastest published
+    mode is faster-evgen + f32): the same draws and accept decisions, FP32
+    physics with the certified cut decisions, so the selected counts equal
+    the FP64 run's batch by batch and the sums agree to FP32 accuracy."""
+    cfg = cfg_sqrts1000.replace(num_events=1_000_000)
+    nb = cfg.num_batches
+    ctx.recheck_count(reset=True)
+    f32 = ctx.run_batches(cfg, 0, nb, rng=rng, jump_per_batch=jump, precision=tp.TP_PREC_FP32_MIXED,
+                          faster_evgen=True)
+    rechecked = ctx.recheck_count(reset=True)
+    f64 = ctx.run_batches(cfg, 0, nb, rng=rng, jump_per_batch=jump, faster_evgen=True)
+    assert np.array_equal(f32.selected, f64.selected)
+    assert 0 < rechecked < 1e-3 * cfg.num_events
+    for name in ("sigma", "variance"):
+        a, b = getattr(f32, name), getattr(f64, name)
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-5, name
+
+
+@pytest.mark.parametrize("rng", ["xoshiro", "ranf"])
+def test_fp32_mixed_res_data_within_1e6(tp, ctx, cfg_valeurs, rng):
+    """res.data of a faster-evgen run at the reference's `valeurs` (1e7
+    events) in FP32-mixed against FP64: the same selected events, every
+    quantity within 1e-6 (the significances' uncertainties 1e-5, as for the
+    default generator)."""
+    r32 = tp.run_simulation(cfg_valeurs, rng=rng, precision=tp.TP_PREC_FP32_MIXED, ctx=ctx, faster_evgen=True)
+    r64 = tp.run_simulation(cfg_valeurs, rng=rng, ctx=ctx, faster_evgen=True)
+    assert r32.selected_events == r64.selected_events
+    for f in ("sigma", "beta_min", "ss_p", "ss_m", "prec", "inc_ss_p", "inc_ss_m"):
+        a, b = getattr(r32, f), getattr(r64, f)
+        assert abs(a - b) <= (1e-5 if f.startswith("inc_") else 1e-6) * abs(b), (f, a, b)
+    for s in range(2):
+        for c in range(5):
+            a, b = r32.spm2[s, c], r64.spm2[s, c]
+            scale = abs(b) if c < 3 else max(abs(b), np.sqrt(abs(r64.spm2[s, 0] * r64.spm2[s, 1])))
+            assert abs(a - b) <= 1e-6 * scale, (s, c, a, b)
