@@ -238,8 +238,9 @@ def compact_line(d, detail_path=None):
             out[key] = {k: v for k, v in d[key].items() if k in ("value", "e2e", "events_per_step", "fp64", "fp32",
                                                                  "fp32_over_xoshiro")}
     if "faster_evgen" in d:
-        out["faster_evgen"] = {x["rng"]: {"events_per_s": x["events_per_s"], "boundary_ms": x["boundary_pass_ms"],
-                                          "ms": x["ms_per_step"]} for x in d["faster_evgen"]}
+        out["faster_evgen"] = {"%s_%s" % (x["rng"], x.get("precision", "fp64")):
+                               {"events_per_s": x["events_per_s"], "boundary_ms": x["boundary_pass_ms"],
+                                "ms": x["ms_per_step"]} for x in d["faster_evgen"]}
     out["detail"] = detail_path
     out["fp32_mixed_value"] = f["value"]
     out["fp32_mixed_e2e"] = f["e2e"]["value"] if "e2e" in f else None
@@ -481,7 +482,7 @@ def grad_leg(tp, ctx, args, events, fit_steps=200):
     return out
 
 
-def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=None):
+def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=None, precision=0):
     """`--features faster-evgen` (TP_MODE_FASTER_EVGEN), FP64, one stream:
     the boundary pass (chunk maps, host composition, thread start states)
     plus the event kernel, timed on the device around the whole call."""
@@ -493,7 +494,8 @@ def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=
             f.data_ptr() + 11 * nb * 8]
 
     def step():
-        ctx.run_batches_device(cfg, 0, nb, ptrs, stream=stream.cuda_stream, rng=rng, seed=seed, faster_evgen=True)
+        ctx.run_batches_device(cfg, 0, nb, ptrs, stream=stream.cuda_stream, rng=rng, seed=seed, faster_evgen=True,
+                               precision=precision)
 
     step()
     torch.cuda.synchronize()
@@ -509,7 +511,8 @@ def faster_evgen_leg(tp, ctx, torch, dev, stream, events, rng, seed, fp64_value=
     ev_ms, _, _, _ = ctx.profile_read()
     ctx.profile(False)
     ms = a.elapsed_time(b) / steps
-    out = {"rng": rng, "events": events, "ms_per_step": ms, "events_per_s": events / (ms * 1e-3),
+    out = {"rng": rng, "precision": "fp32_mixed" if precision else "fp64", "events": events, "ms_per_step": ms,
+           "events_per_s": events / (ms * 1e-3),
            "event_kernel_ms": ev_ms / steps, "boundary_pass_ms": ms - ev_ms / steps,
            "selected": int(sel.sum().item())}
     if fp64_value:
@@ -803,7 +806,11 @@ def main():
         line["ranf"] = ranf_leg(tp, ctx, torch, dev, stream, events, fp32["value"])
         line["faster_evgen"] = [faster_evgen_leg(tp, ctx, torch, dev, stream, events, "xoshiro", SEED, value),
                                 faster_evgen_leg(tp, ctx, torch, dev, stream, events // 5, "ranf",
-                                                 tp.RANF_DEFAULT_SEED)]
+                                                 tp.RANF_DEFAULT_SEED),
+                                faster_evgen_leg(tp, ctx, torch, dev, stream, events, "xoshiro", SEED,
+                                                 precision=tp.TP_PREC_FP32_MIXED),
+                                faster_evgen_leg(tp, ctx, torch, dev, stream, events // 5, "ranf",
+                                                 tp.RANF_DEFAULT_SEED, precision=tp.TP_PREC_FP32_MIXED)]
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(tp)
     if args.detail:
