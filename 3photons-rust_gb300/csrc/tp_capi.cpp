@@ -462,7 +462,7 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
         }
         if (m == kFeMapError)
           return c->fail(TP_ERR_DEVICE, "faster-evgen: an event runs past its chunk's accept bits");
-        s.chunks.push_back(FeChunk{s.id, s.next_chunk, s.events, s.entry, 0});
+        s.chunks.push_back(FeChunk{s.id, s.next_chunk, s.events, s.entry, m & 0xffffu});
         s.events += m & 0xffffu;
         s.entry = m >> 16;
         ++s.next_chunk;
@@ -516,7 +516,8 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     // the map pass keeps every chunk's accept bits (and xoshiro lane states)
     // for the starts pass when they fit in kFeStoreCap (5.2 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
-    const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t);
+    const size_t per_chunk =
+        kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t) + 32 * kFeCps * sizeof(uint32_t);
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
         return st;
@@ -524,6 +525,8 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
       fp.lane_store = reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
                                                   chunks * kFeStoreWords * sizeof(uint32_t));
       fp.store_chunks = chunks;
+      fp.cp_store = reinterpret_cast<uint32_t*>(static_cast<char*>(c->d_fe_store) +
+                                                chunks * (kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t)));
     }
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }

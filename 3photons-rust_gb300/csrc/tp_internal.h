@@ -135,7 +135,7 @@ struct FeChunk {
   uint64_t chunk;   // positions [chunk * kFeChunk, ...) of the stream
   uint64_t first_event;
   uint32_t entry;
-  uint32_t pad;
+  uint32_t events;  // starts pass: events that start in the chunk (from the composition)
 };
 
 struct FeParams {
@@ -166,8 +166,14 @@ struct FeParams {
   uint32_t* bits_store;
   uint64_t* lane_store;
   uint64_t store_chunks;
+  // and, for each of a chunk's 32 chases, the position and residue mod 55
+  // (P | r << 16) of every kFeCpEvery-th event start (kFeCps per chase)
+  uint32_t* cp_store;
 };
 constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32);
+constexpr uint32_t kFeCpEvery = 128;
+constexpr int kFeCps = 18;        // > (kFeChunk / 15 + 1) / kFeCpEvery: a chunk holds at most 2185 event starts
+constexpr int kFeLaneRecs = 8;    // thread starts in one lane's 128 events (at most 128 / 40 + 2)
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
