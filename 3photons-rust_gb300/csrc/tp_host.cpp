@@ -265,11 +265,25 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   k.f_fx_ep = (float)k.fx_ep;
   k.f_c1 = (float)k.c1;
   k.f_c2 = (float)k.c2;
-  for (int c = 0; c < 4; ++c) k.f_sc_raw[c] = (float)k.sc_raw[c];
+  // the FP32 sums' scaling: momenta in units of lambda (a power of 2 at
+  // least the beam energy); with gamma = xx_in lambda the five sums are
+  // homogeneous of degrees gamma^-4 lambda^2, gamma^4 lambda^2 (twice) and
+  // lambda^2 (twice) in the spinor normalisation
+  int lexp = 0;
+  std::frexp(k.half, &lexp);  // half = f 2^lexp, 0.5 <= f < 1
+  const double lambda = std::ldexp(1.0, lexp);
+  const double gamma = k.xx_in * lambda, g4 = gamma * gamma * gamma * gamma, l2 = lambda * lambda;
+  const double hat[5] = {l2 / g4, g4 * l2, g4 * l2, l2, l2};
+  k.f_inv_lambda = (float)(1.0 / lambda);
+  for (int c = 0; c < 5; ++c) {
+    k.hat_scale[c] = hat[c];
+    k.f_sc_raw[c] = (float)(k.sc_raw[c < 3 ? c : 3] * hat[c]);
+    k.f_raw_to_hat[c] = (float)(1.0 / hat[c]);
+  }
   for (int c = 0; c < 5; ++c) k.f_sc[c] = (float)k.sc[c];
   for (int c = 0; c < 5; ++c) {
     k.K[c] = k.sc_raw[c < 3 ? c : 3] * k.sc[c];
-    k.f_K[c] = (float)k.K[c];
+    k.f_K[c] = (float)(k.K[c] * hat[c]);
   }
   k.flags = flags;
   *out = k;

@@ -40,7 +40,15 @@ struct EvConst {
   // FP32 copies for the mixed-precision path
   float f_e_total, f_half, f_em_x, f_acut, f_bcut, f_emin, f_sincut;
   float f_xx_in, f_fx_em, f_fx_ep, f_c1, f_c2;
-  float f_sc_raw[4];
+  // The FP32 helicity sums are computed from momenta scaled by 1 / lambda,
+  // lambda = 2^ceil(log2(sqrt(s) / 2)) (exact), and come out as raw_c /
+  // hat_scale[c] (each sum is homogeneous in the momenta); f_sc_raw, f_K
+  // include hat_scale, f_raw_to_hat = 1 / hat_scale (the direct formulas'
+  // sums into the scaled ones)
+  float f_inv_lambda;
+  float f_sc_raw[5];
+  float f_raw_to_hat[5];
+  double hat_scale[5];
   float f_sc[5];
   // per-event weight w = sum_c raw_c * K_c (K = sc_raw * sc, see above)
   double K[5];
