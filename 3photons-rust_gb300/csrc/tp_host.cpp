@@ -277,13 +277,15 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   k.f_inv_lambda = (float)(1.0 / lambda);
   for (int c = 0; c < 5; ++c) {
     k.hat_scale[c] = hat[c];
-    k.f_sc_raw[c] = (float)(k.sc_raw[c < 3 ? c : 3] * hat[c]);
+    k.sc_raw_hat[c] = k.sc_raw[c < 3 ? c : 3] * hat[c];
+    k.f_sc_raw[c] = (float)k.sc_raw_hat[c];
     k.f_raw_to_hat[c] = (float)(1.0 / hat[c]);
   }
   for (int c = 0; c < 5; ++c) k.f_sc[c] = (float)k.sc[c];
   for (int c = 0; c < 5; ++c) {
     k.K[c] = k.sc_raw[c < 3 ? c : 3] * k.sc[c];
     k.f_K[c] = (float)(k.K[c] * hat[c]);
+    k.f_K_lo[c] = (float)(k.K[c] * hat[c] - (double)k.f_K[c]);
   }
   k.flags = flags;
   *out = k;

@@ -49,6 +49,12 @@ struct EvConst {
   float f_sc_raw[5];
   float f_raw_to_hat[5];
   double hat_scale[5];
+  // the FP32 batch sums are taken on the scaled sums and multiplied by
+  // sc_raw_hat (and its square) in FP64 at the batch reduction; the event
+  // weight uses f_K + f_K_lo, K's FP32 rounding and its remainder, so that
+  // no constant's FP32 rounding biases the sums
+  double sc_raw_hat[5];
+  float f_K_lo[5];
   float f_sc[5];
   // per-event weight w = sum_c raw_c * K_c (K = sc_raw * sc, see above)
   double K[5];
