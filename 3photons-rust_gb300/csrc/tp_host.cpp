@@ -280,6 +280,7 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
     k.sc_raw_hat[c] = k.sc_raw[c < 3 ? c : 3] * hat[c];
     k.f_sc_raw[c] = (float)k.sc_raw_hat[c];
     k.f_raw_to_hat[c] = (float)(1.0 / hat[c]);
+    k.f_raw_to_hat_lo[c] = (float)(1.0 / hat[c] - (double)k.f_raw_to_hat[c]);
   }
   for (int c = 0; c < 5; ++c) k.f_sc[c] = (float)k.sc[c];
   for (int c = 0; c < 5; ++c) {

@@ -47,7 +47,7 @@ struct EvConst {
   // sums into the scaled ones)
   float f_inv_lambda;
   float f_sc_raw[5];
-  float f_raw_to_hat[5];
+  float f_raw_to_hat[5], f_raw_to_hat_lo[5];
   double hat_scale[5];
   // the FP32 batch sums are taken on the scaled sums and multiplied by
   // sc_raw_hat (and its square) in FP64 at the batch reduction; the event
