@@ -423,7 +423,27 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   fp.map = static_cast<uint32_t*>(c->d_fe_map);
   if (launch_fe_seed(fp, stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen seed launch: ") + cudaGetErrorString(cudaGetLastError()));
-  if ((map_pass ? launch_fe_map(fp, stream) : launch_fe_starts(fp, stream)) != TP_OK)
+  // chunks inside the store (a prefix of the launch: its chunks ascend) map
+  // by sub-spans and keep their bits, lane states and traces for the starts
+  // pass; the rest take the lockstep chase
+  size_t n_sub = 0;
+  if (map_pass && fp.bits_store && !fp.jpb)
+    while (n_sub < n && descs[n_sub].chunk < fp.store_chunks) ++n_sub;
+  int lst = TP_OK;
+  if (!map_pass) {
+    lst = launch_fe_starts(fp, stream);
+  } else {
+    FeParams sub = fp, rest = fp;
+    sub.n_chunks = n_sub;
+    rest.n_chunks = n - n_sub;
+    rest.chunks += n_sub;
+    rest.map += n_sub * kFeEntries;
+    rest.chunk_state = static_cast<char*>(c->d_fe_cstate) +
+                       n_sub * (fp.kind == TP_RNG_RANF ? 56 * sizeof(int32_t) : 4 * sizeof(uint64_t));
+    lst = launch_fe_map_sub(sub, stream);
+    if (lst == TP_OK) lst = launch_fe_map(rest, stream);
+  }
+  if (lst != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen chunk launch: ") + cudaGetErrorString(cudaGetLastError()));
   if (!map_pass) return TP_OK;
   maps->resize(n * kFeEntries);
@@ -517,7 +537,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     // for the starts pass when they fit in kFeStoreCap (5.2 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
     const size_t per_chunk =
-        kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t) + 32 * kFeCps * sizeof(uint32_t);
+        kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t) + 32 * kFeSubs * sizeof(uint16_t);
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
         return st;
@@ -525,8 +545,8 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
       fp.lane_store = reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
                                                   chunks * kFeStoreWords * sizeof(uint32_t));
       fp.store_chunks = chunks;
-      fp.cp_store = reinterpret_cast<uint32_t*>(static_cast<char*>(c->d_fe_store) +
-                                                chunks * (kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t)));
+      fp.trace_store = reinterpret_cast<uint16_t*>(static_cast<char*>(c->d_fe_store) +
+                                                   chunks * (kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t)));
     }
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }

@@ -180,14 +180,17 @@ struct FeParams {
   uint32_t* bits_store;
   uint64_t* lane_store;
   uint64_t store_chunks;
-  // and, for each of a chunk's 32 chases, the position and residue mod 55
-  // (P | r << 16) of every kFeCpEvery-th event start (kFeCps per chase)
-  uint32_t* cp_store;
+  // and, for each of a chunk's 32 entry offsets, its trace through the
+  // chunk's kFeSubs sub-spans: entry offset | events << 8 per sub-span
+  uint16_t* trace_store;
 };
 constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32);
-constexpr uint32_t kFeCpEvery = 128;
-constexpr int kFeCps = 18;        // > (kFeChunk / 15 + 1) / kFeCpEvery: a chunk holds at most 2185 event starts
-constexpr int kFeLaneRecs = 8;    // thread starts in one lane's 128 events (at most 128 / 40 + 2)
+constexpr int kFeSubs = 64;                          // sub-spans per chunk (map pass)
+constexpr uint32_t kFeSub = kFeChunk / kFeSubs;      // 512 positions: at most 35 event starts
+constexpr int kFeFams = 4;                           // exit families per sub-span
+constexpr int kFePath = 40;                          // events of one chase within a sub-span
+constexpr uint16_t kFeTraceInvalid = 0xffff;         // trace not kept (the chunk took the lockstep chase)
+constexpr int kFeLaneRecs = 8;    // thread starts in a lane's two sub-spans (at most 2 (35 / 40 + 2))
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
@@ -227,6 +230,7 @@ int launch_adjoint(int rng_kind, const KParams& p, int tpb, void* stream);
 // events (batch_state = the thread start states)
 int launch_fe_seed(const FeParams& p, void* stream);
 int launch_fe_map(const FeParams& p, void* stream);
+int launch_fe_map_sub(const FeParams& p, void* stream);  // k_fe_bits + k_fe_map_sub (bit store kept)
 int launch_fe_starts(const FeParams& p, void* stream);
 int launch_fe_events(int rng_kind, const KParams& p, int tpb, void* stream);
 
