@@ -378,7 +378,8 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // event's first draw is found before the physics:
 //  1. map pass: per chunk of kFeChunk draw positions, for 32 entry offsets,
 //     the offset where the chunk's last event ends and the chunk's event
-//     count (k_fe_map, one warp per chunk, from the accept bits);
+//     count (k_fe_map, one CTA per chunk: the accept bits, the sub-span
+//     chases and a walk per entry offset);
 //  2. on the host, the maps composed along each stream from draw 0: the
 //     first event and its offset in every chunk;
 //  3. starts pass: per chunk, the stream state at each thread's first event
@@ -388,7 +389,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
 constexpr uint64_t kFeMapLaunch = 16384;  // chunks per map launch
-constexpr uint64_t kFeStoreCap = 8ull << 30;  // bytes of device memory for the bit store
+constexpr uint64_t kFeStoreCap = 16ull << 30;  // bytes of device memory for the bit store
 // batches per starts + events launch: bounds the thread start states to
 // 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
 constexpr uint64_t kFePieceXo = 16384, kFePieceRanf = 4096;
@@ -423,26 +424,7 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   fp.map = static_cast<uint32_t*>(c->d_fe_map);
   if (launch_fe_seed(fp, stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen seed launch: ") + cudaGetErrorString(cudaGetLastError()));
-  // chunks inside the store (a prefix of the launch: its chunks ascend) map
-  // by sub-spans and keep their bits, lane states and traces for the starts
-  // pass; the rest take the lockstep chase
-  size_t n_sub = 0;
-  if (map_pass && fp.bits_store && !fp.jpb)
-    while (n_sub < n && descs[n_sub].chunk < fp.store_chunks) ++n_sub;
-  int lst = TP_OK;
-  if (!map_pass) {
-    lst = launch_fe_starts(fp, stream);
-  } else {
-    FeParams sub = fp, rest = fp;
-    sub.n_chunks = n_sub;
-    rest.n_chunks = n - n_sub;
-    rest.chunks += n_sub;
-    rest.map += n_sub * kFeEntries;
-    rest.chunk_state = static_cast<char*>(c->d_fe_cstate) +
-                       n_sub * (fp.kind == TP_RNG_RANF ? 56 * sizeof(int32_t) : 4 * sizeof(uint64_t));
-    lst = launch_fe_map_sub(sub, stream);
-    if (lst == TP_OK) lst = launch_fe_map(rest, stream);
-  }
+  const int lst = map_pass ? launch_fe_map(fp, stream) : launch_fe_starts(fp, stream);
   if (lst != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen chunk launch: ") + cudaGetErrorString(cudaGetLastError()));
   if (!map_pass) return TP_OK;
@@ -534,19 +516,19 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
     // the map pass keeps every chunk's accept bits (and xoshiro lane states)
-    // for the starts pass when they fit in kFeStoreCap (5.2 GB per 1e9 events)
+    // for the starts pass when they fit in kFeStoreCap (xoshiro 12.8 GB and
+    // ranf 7.6 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
-    const size_t per_chunk =
-        kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t) + 32 * kFeSubs * sizeof(uint16_t);
+    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? 32 * kFeCkpts * 4 * sizeof(uint64_t) : 0;
+    const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + ckpt_bytes;
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
         return st;
       fp.bits_store = static_cast<uint32_t*>(c->d_fe_store);
-      fp.lane_store = reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
-                                                  chunks * kFeStoreWords * sizeof(uint32_t));
+      fp.ckpt_store = ckpt_bytes ? reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
+                                                               chunks * kFeStoreWords * sizeof(uint32_t))
+                                 : nullptr;
       fp.store_chunks = chunks;
-      fp.trace_store = reinterpret_cast<uint16_t*>(static_cast<char*>(c->d_fe_store) +
-                                                   chunks * (kFeStoreWords * sizeof(uint32_t) + 32 * 4 * sizeof(uint64_t)));
     }
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }
@@ -1214,7 +1196,9 @@ int tp_profile_read(tp_ctx* c, double* event_ms, uint64_t* event_launches, doubl
 
 namespace {
 // seconds per operation of k_probe's op `op` (chains per thread: 16 for the
-// FMA ops 0 and 5, else 8), timed until a launch lasts 20 ms
+// FMA ops 0 and 5, else 8), timed until a launch lasts 20 ms. One untimed
+// launch comes first: the first launch of a kernel also loads its module
+// (lazy loading), which can take longer than the 20 ms mark by itself.
 int probe_op_seconds(tp_ctx* c, int op, double* seconds) {
   int sms = 0;
   if (int st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "probe")) return st;
@@ -1224,9 +1208,10 @@ int probe_op_seconds(tp_ctx* c, int op, double* seconds) {
   const int blocks = sms * 8, tpb = 256;
   const double threads = (double)blocks * tpb;
   const double chains = (op == 0 || op == 5) ? 16.0 : 8.0;
-  int st = TP_OK;
+  int st = launch_probe(op, 1, blocks, tpb, sink, c->stream);
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "probe");
   int iters = 16;
-  for (int rep = 0; rep < 8; ++rep) {
+  for (int rep = 0; rep < 8 && !st; ++rep) {
     cudaEventRecord(a, c->stream);
     st = launch_probe(op, iters, blocks, tpb, sink, c->stream);
     cudaEventRecord(b, c->stream);
@@ -1261,37 +1246,9 @@ int tp_probe_fp32(tp_ctx* c, double out[2]) {
 int tp_probe_fp64(tp_ctx* c, double out[5]) {
   if (!c || !out) return TP_ERR_INVALID;
   cudaSetDevice(c->device);
-  int sms = 0;
-  if (int st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "probe")) return st;
-  double* sink = nullptr;
-  if (int st = c->cuda(cudaMalloc(&sink, sizeof(double)), "probe")) return st;
-  cudaEvent_t a = c->next_event(), b = c->next_event();
-  const int blocks = sms * 8, tpb = 256;
-  const double threads = (double)blocks * tpb;
   double per_op_s[5];
-  int st = TP_OK;
-  for (int op = 0; op < 5 && st == TP_OK; ++op) {
-    int iters = 16;
-    for (int rep = 0; rep < 8; ++rep) {
-      cudaEventRecord(a, c->stream);
-      st = launch_probe(op, iters, blocks, tpb, sink, c->stream);
-      cudaEventRecord(b, c->stream);
-      if (!st) st = c->cuda(cudaEventSynchronize(b), "probe");
-      if (st) break;
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms > 20.f || rep == 7) {
-        const double chains = op == 0 ? 16.0 : 8.0;  // independent chains per thread (k_probe)
-        per_op_s[op] = (ms * 1e-3) / (threads * chains * iters);  // seconds per operation
-        break;
-      }
-      const double grow = ms > 0.01f ? 25.0 / ms : 64.0;
-      iters = (int)(iters * (grow > 64.0 ? 64.0 : grow)) + 1;
-    }
-  }
-  cudaFree(sink);
-  c->ev_used = 0;
-  if (st) return st;
+  for (int op = 0; op < 5; ++op)
+    if (int st = probe_op_seconds(c, op, &per_op_s[op])) return st;
   out[0] = 2.0 / per_op_s[0];  // DFMA flop/s
   for (int op = 1; op < 5; ++op) out[op] = per_op_s[op] / per_op_s[0];  // DFMA equivalents
   return TP_OK;

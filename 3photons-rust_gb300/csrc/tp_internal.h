@@ -126,9 +126,9 @@ struct PointsParams {
 // faster-evgen (src/evgen.rs:143-173, 221-249): an event takes 15 draws plus
 // 2 per rejected point, so event boundaries are found before the physics.
 // A stream's draw positions are cut into chunks of kFeChunk; an event
-// belongs to the chunk of its first draw. One warp per chunk computes the
-// accept bits of kFeSpan positions (the chunk and a margin for the events
-// that run past its end), 1152 per lane.
+// belongs to the chunk of its first draw. Warp 0 of a chunk's CTA computes
+// the accept bits of kFeSpan positions (the chunk and a margin for the
+// events that run past its end), 1152 per lane.
 constexpr uint32_t kFeChunk = 32768;
 constexpr uint32_t kFeSpan = 36864;
 constexpr uint32_t kFeLaneSpan = kFeSpan / 32;
@@ -141,7 +141,7 @@ constexpr unsigned kFeErrSpan = 0x10u;     // an event ran past the chunk's span
 constexpr unsigned kFeErrStarts = 0x20u;   // too many thread starts in a chunk
 constexpr unsigned kFeErrTries = 0x40u;    // a point was re-rolled kFeMaxTries times
 
-// One chunk of a stream: for the map pass, lane l chases entry offset
+// One chunk of a stream: for the map pass, lane l maps entry offset
 // entry + l; for the starts pass, entry is the offset of the chunk's first
 // event and first_event its index within the stream.
 struct FeChunk {
@@ -173,24 +173,24 @@ struct FeParams {
   int ept, tpb;
   void* thread_state;
   unsigned int* err;
-  // one-stream runs: the map pass keeps each chunk's accept bits
-  // (kFeStoreWords words) and, for xoshiro, its lanes' span-start states
-  // (32 x 4 words) for the starts pass; chunks >= store_chunks (or a null
-  // store) regenerate them
+  // one-stream runs: the map pass keeps each chunk's accept bits and
+  // sub-span chases (kFeStoreWords words) and, for xoshiro, its lanes'
+  // checkpoints (32 x kFeCkpts x 4 words) for the starts pass; chunks >=
+  // store_chunks (or a null store) regenerate them
   uint32_t* bits_store;
-  uint64_t* lane_store;
+  uint64_t* ckpt_store;
   uint64_t store_chunks;
-  // and, for each of a chunk's 32 entry offsets, its trace through the
-  // chunk's kFeSubs sub-spans: entry offset | events << 8 per sub-span
-  uint16_t* trace_store;
 };
-constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32);
-constexpr int kFeSubs = 64;                          // sub-spans per chunk (map pass)
-constexpr uint32_t kFeSub = kFeChunk / kFeSubs;      // 512 positions: at most 35 event starts
-constexpr int kFeFams = 4;                           // exit families per sub-span
-constexpr int kFePath = 40;                          // events of one chase within a sub-span
-constexpr uint16_t kFeTraceInvalid = 0xffff;         // trace not kept (the chunk took the lockstep chase)
-constexpr int kFeLaneRecs = 8;    // thread starts in a lane's two sub-spans (at most 2 (35 / 40 + 2))
+// The chunk kernels chase each of kFeSubs sub-spans of kFeSub positions
+// (one lane each) from kFeLead positions before it; a walk through the
+// chunk then jumps over every sub-span whose chase it meets.
+constexpr int kFeSubs = 32;
+constexpr uint32_t kFeSub = kFeChunk / kFeSubs;  // 1024 positions
+constexpr uint32_t kFeLead = 2048;
+// bit store words per chunk: bits A and B, the chases' marks and exits
+constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32) + kFeChunk / 32 + kFeSubs;
+// xoshiro checkpoints per lane: the states at 1152 l + 128 k + 3, k < 9
+constexpr uint32_t kFeCkpts = 9;
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
@@ -230,7 +230,6 @@ int launch_adjoint(int rng_kind, const KParams& p, int tpb, void* stream);
 // events (batch_state = the thread start states)
 int launch_fe_seed(const FeParams& p, void* stream);
 int launch_fe_map(const FeParams& p, void* stream);
-int launch_fe_map_sub(const FeParams& p, void* stream);  // k_fe_bits + k_fe_map_sub (bit store kept)
 int launch_fe_starts(const FeParams& p, void* stream);
 int launch_fe_events(int rng_kind, const KParams& p, int tpb, void* stream);
 
