@@ -286,7 +286,6 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   for (int c = 0; c < 5; ++c) {
     k.K[c] = k.sc_raw[c < 3 ? c : 3] * k.sc[c];
     k.f_K[c] = (float)(k.K[c] * hat[c]);
-    k.f_K_lo[c] = (float)(k.K[c] * hat[c] - (double)k.f_K[c]);
   }
   k.flags = flags;
   *out = k;

@@ -50,11 +50,10 @@ struct EvConst {
   float f_raw_to_hat[5], f_raw_to_hat_lo[5];
   double hat_scale[5];
   // the FP32 batch sums are taken on the scaled sums and multiplied by
-  // sc_raw_hat (and its square) in FP64 at the batch reduction; the event
-  // weight uses f_K + f_K_lo, K's FP32 rounding and its remainder, so that
-  // no constant's FP32 rounding biases the sums
+  // sc_raw_hat (and its square) in FP64 at the batch reduction, which also
+  // forms sigma from them with K hat_scale in FP64; only the squared event
+  // weight (the variance) uses K's FP32 rounding f_K
   double sc_raw_hat[5];
-  float f_K_lo[5];
   float f_sc[5];
   // per-event weight w = sum_c raw_c * K_c (K = sc_raw * sc, see above)
   double K[5];
