@@ -36,7 +36,7 @@ constexpr int kBinnedEpt = 313;  // binned passes: one warp per batch (measured 
 struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
   std::vector<uint64_t> xo_fe_chunk;                  // 64 x 4: x^(kFeChunk 2^k)
-  std::vector<uint64_t> xo_fe_lane;                   // 32 x 4: x^(kFeLaneSpan l)
+  std::vector<uint64_t> xo_fe_lane;                   // kFeThreads x 4: x^(kFeLaneSpan l)
   std::vector<uint32_t> ranf;                         // 64 x 55
 };
 
@@ -64,10 +64,10 @@ const Tables& host_tables() {
       for (int w = 0; w < 4; ++w) t.xo_fe_chunk[4 * k + w] = pc.w[w];
       pc = gf2_mulmod(pc, pc);
     }
-    t.xo_fe_lane.resize(128);
+    t.xo_fe_lane.resize(4 * kFeThreads);
     const Gf2Poly lane_step = gf2_xpow(kFeLaneSpan);
     Gf2Poly cur{{1, 0, 0, 0}};
-    for (int l = 0; l < 32; ++l) {
+    for (int l = 0; l < kFeThreads; ++l) {
       for (int w = 0; w < 4; ++w) t.xo_fe_lane[4 * l + w] = cur.w[w];
       cur = gf2_mulmod(cur, lane_step);
     }
@@ -116,6 +116,7 @@ struct tp_ctx {
   // faster-evgen: jump tables, chunk list, chunk states, chunk maps, thread start states
   uint64_t* d_xo_fe_chunk = nullptr;
   uint64_t* d_xo_fe_lane = nullptr;
+  uint64_t* d_fe_lane_tab = nullptr;  // the lane jumps as tables (2 MiB)
   void* d_fe_chunks = nullptr;
   size_t fe_chunks_bytes = 0;
   void* d_fe_cstate = nullptr;
@@ -388,7 +389,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // One stream (events numbered through the run) or one per batch
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
-constexpr uint64_t kFeMapLaunch = 16384;  // chunks per map launch
+constexpr uint64_t kFeMapLaunch = 65536;  // chunks per map launch
 constexpr uint64_t kFeStoreCap = 16ull << 30;  // bytes of device memory for the bit store
 // batches per starts + events launch: bounds the thread start states to
 // 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
@@ -443,8 +444,10 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
     descs.clear();
     for (FeStream& s : streams) {
       if (s.done()) continue;
-      // ~16.6 (xoshiro) or ~17.9 (ranf, block skips) draws per event; two chunks of slack
-      const uint64_t need = (uint64_t)((double)(s.target - s.events) * 18.5 / kFeChunk) + 2;
+      // ~16.64 (xoshiro) or ~17.9 (ranf, block skips) draws per event; a
+      // short guess maps the rest in the next round
+      const double draws = fp.kind == TP_RNG_RANF ? 18.0 : 16.7;
+      const uint64_t need = (uint64_t)((double)(s.target - s.events) * draws / kFeChunk) + 2;
       for (uint64_t k = 0; k < need && descs.size() < kFeMapLaunch; ++k)
         descs.push_back(FeChunk{s.id, s.next_chunk + k, 0, 0, 0});
       if (descs.size() >= kFeMapLaunch) break;
@@ -499,7 +502,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
   fp.ranf_table = c->d_ranf_tab;
   fp.xo_stream = c->d_xo_jump;
   fp.xo_chunk = c->d_xo_fe_chunk;
-  fp.xo_lane = c->d_xo_fe_lane;
+  fp.xo_lane_tab = c->d_fe_lane_tab;
   KParams kp{};
   make_ev_const(*cfg, rng_kind & ~TP_RNG_KIND_MASK, &kp.k);
   kp.num_events = n_total;
@@ -516,10 +519,10 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
     // the map pass keeps every chunk's accept bits (and xoshiro lane states)
-    // for the starts pass when they fit in kFeStoreCap (xoshiro 12.8 GB and
-    // ranf 7.6 GB per 1e9 events)
+    // for the starts pass when they fit in kFeStoreCap (xoshiro 15.7 GB and
+    // ranf 9.9 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
-    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? 32 * kFeCkpts * 4 * sizeof(uint64_t) : 0;
+    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? kFeThreads * kFeCkpts * 4 * sizeof(uint64_t) : 0;
     const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + ckpt_bytes;
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
@@ -655,7 +658,8 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_binw, kMaxBins * sizeof(double), "bin weights");
   alloc((void**)&c->d_adj, kChunk * 10 * sizeof(double), "adjoint sums");
   alloc((void**)&c->d_xo_fe_chunk, 256 * 8, "tables");
-  alloc((void**)&c->d_xo_fe_lane, 128 * 8, "tables");
+  alloc((void**)&c->d_xo_fe_lane, 4 * kFeThreads * 8, "tables");
+  alloc((void**)&c->d_fe_lane_tab, (size_t)kFeThreads * kJumpTabWords * 8, "jump tables");
   if (!st) st = c->cuda(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "device query");
   alloc(&c->d_state, kChunk * 56 * 4, "batch states");
   (void)dummy;
@@ -666,7 +670,12 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st) st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), 64 * 55 * 4, cudaMemcpyHostToDevice), "tables");
   if (!st)
     st = c->cuda(cudaMemcpy(c->d_xo_fe_chunk, t.xo_fe_chunk.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
-  if (!st) st = c->cuda(cudaMemcpy(c->d_xo_fe_lane, t.xo_fe_lane.data(), 128 * 8, cudaMemcpyHostToDevice), "tables");
+  if (!st)
+    st = c->cuda(cudaMemcpy(c->d_xo_fe_lane, t.xo_fe_lane.data(), 4 * kFeThreads * 8, cudaMemcpyHostToDevice),
+                 "tables");
+  if (!st && launch_build_jump_tab(c->d_xo_fe_lane, kFeThreads, c->d_fe_lane_tab, c->stream) != TP_OK)
+    st = c->fail(TP_ERR_CUDA, "faster-evgen lane tables: launch failed");
+  if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "faster-evgen lane tables");
   if (!st) st = c->cuda(cudaMemset(c->d_err, 0, sizeof(unsigned int)), "error word");
   if (!st) st = c->cuda(cudaMemset(c->d_recheck, 0, sizeof(unsigned long long)), "recheck counter");
   if (st) {
@@ -687,7 +696,7 @@ void tp_destroy(tp_ctx* c) {
                   c->d_thread_poly[0], c->d_thread_poly[1], c->d_thread_poly[2],
                   c->d_jump_tab[0], c->d_jump_tab[1], c->d_jump_tab[2],
                   c->d_ranf_window, c->d_state, c->d_out, c->d_dump, c->d_err, c->d_recheck,
-                  c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_chunks,
+                  c->d_hist, c->d_binw, c->d_adj, c->d_xo_fe_chunk, c->d_xo_fe_lane, c->d_fe_lane_tab, c->d_fe_chunks,
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
   for (void* b : bufs)
     if (b) cudaFree(b);

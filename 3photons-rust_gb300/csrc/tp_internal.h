@@ -125,12 +125,13 @@ struct PointsParams {
 // faster-evgen (src/evgen.rs:143-173, 221-249): an event takes 15 draws plus
 // 2 per rejected point, so event boundaries are found before the physics.
 // A stream's draw positions are cut into chunks of kFeChunk; an event
-// belongs to the chunk of its first draw. Warp 0 of a chunk's CTA computes
-// the accept bits of kFeSpan positions (the chunk and a margin for the
-// events that run past its end), 1152 per lane.
+// belongs to the chunk of its first draw. A chunk's CTA (two warps)
+// computes the accept bits of kFeSpan positions (the chunk and a margin for
+// the events that run past its end), 576 per xoshiro lane.
 constexpr uint32_t kFeChunk = 32768;
 constexpr uint32_t kFeSpan = 36864;
-constexpr uint32_t kFeLaneSpan = kFeSpan / 32;
+constexpr int kFeThreads = 64;  // threads of the chunk kernels
+constexpr uint32_t kFeLaneSpan = kFeSpan / kFeThreads;
 constexpr int kFeEntries = 32;             // entry offsets per chunk map
 constexpr uint32_t kFeMapError = 0xffffffffu;
 constexpr int kFeMaxStarts = 128;          // thread starts recorded per chunk
@@ -160,7 +161,7 @@ struct FeParams {
   const uint32_t* ranf_table;    // x^(55 2^k) mod P
   const uint64_t* xo_stream;     // x^(2^128 2^k): per-batch stream starts
   const uint64_t* xo_chunk;      // x^(kFeChunk 2^k)
-  const uint64_t* xo_lane;       // x^(kFeLaneSpan l), l < 32
+  const uint64_t* xo_lane_tab;   // x^(kFeLaneSpan l), l < kFeThreads, as jump tables (kJumpTabWords each)
   const FeChunk* chunks;
   uint64_t n_chunks;
   void* chunk_state;             // per chunk: xoshiro 4 x u64, ranf 56 x i32
@@ -174,7 +175,7 @@ struct FeParams {
   unsigned int* err;
   // one-stream runs: the map pass keeps each chunk's accept bits and
   // sub-span chases (kFeStoreWords words) and, for xoshiro, its lanes'
-  // checkpoints (32 x kFeCkpts x 4 words) for the starts pass; chunks >=
+  // checkpoints (kFeThreads x kFeCkpts x 4 words) for the starts pass; chunks >=
   // store_chunks (or a null store) regenerate them
   uint32_t* bits_store;
   uint64_t* ckpt_store;
@@ -186,10 +187,17 @@ struct FeParams {
 constexpr int kFeSubs = 32;
 constexpr uint32_t kFeSub = kFeChunk / kFeSubs;  // 1024 positions
 constexpr uint32_t kFeLead = 2048;
-// bit store words per chunk: bits A and B, the chases' marks and exits
-constexpr uint32_t kFeStoreWords = 2 * (kFeSpan / 32) + kFeChunk / 32 + kFeSubs;
-// xoshiro checkpoints per lane: the states at 1152 l + 128 k + 3, k < 9
-constexpr uint32_t kFeCkpts = 9;
+// bit store words per chunk: bits A and B, the chases' marks and exits,
+// the map pass's walks (per sub-span and entry lane: the walk's first
+// event start in the sub-span | the events before it << 16) and the entry
+// offset of lane 0; 16-byte aligned parts
+constexpr uint32_t kFeStoreCanon = 2 * (kFeSpan / 32);
+constexpr uint32_t kFeStoreExit = kFeStoreCanon + kFeChunk / 32;
+constexpr uint32_t kFeStoreTrace = kFeStoreExit + kFeSubs;
+constexpr uint32_t kFeStoreEntry = kFeStoreTrace + kFeSubs * kFeEntries;
+constexpr uint32_t kFeStoreWords = kFeStoreEntry + 4;
+// xoshiro checkpoints per lane: the states at 576 l + 128 k + 3, k < 5
+constexpr uint32_t kFeCkpts = (kFeLaneSpan / 32 + 3) / 4;
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
