@@ -126,6 +126,8 @@ struct tp_ctx {
   void* d_fe_tstate = nullptr;
   size_t fe_tstate_bytes = 0;
   void* d_fe_store = nullptr;  // one-stream runs: accept bits and lane states per chunk
+  uint32_t* h_fe_maps = nullptr;  // pinned host copy of a map launch's maps
+  size_t h_fe_maps_bytes = 0;
   size_t fe_store_bytes = 0;
   int sms = 0;
   // batched form (tp_run_points): device buffers and the captured graph
@@ -405,9 +407,11 @@ struct FeStream {
   bool done() const { return events >= target; }
 };
 
-// Uploads `descs`, seeds their chunk states and runs `pass` on them.
+// Uploads `descs`, seeds their chunk states and runs the map pass (maps:
+// where the maps are copied back; pinned: into the context's pinned buffer
+// instead, *pinned pointing at them) or the starts pass on them.
 int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool map_pass, cudaStream_t stream,
-              std::vector<uint32_t>* maps) {
+              std::vector<uint32_t>* maps, const uint32_t** pinned = nullptr) {
   const size_t n = descs.size();
   if (n == 0) return TP_OK;
   if (int st = ensure(c, &c->d_fe_chunks, &c->fe_chunks_bytes, n * sizeof(FeChunk), "faster-evgen chunks")) return st;
@@ -429,9 +433,23 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   if (lst != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen chunk launch: ") + cudaGetErrorString(cudaGetLastError()));
   if (!map_pass) return TP_OK;
-  maps->resize(n * kFeEntries);
-  st = c->cuda(cudaMemcpyAsync(maps->data(), c->d_fe_map, n * kFeEntries * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                               stream), "copy faster-evgen maps");
+  const size_t bytes = n * kFeEntries * sizeof(uint32_t);
+  uint32_t* dst = nullptr;
+  if (pinned) {
+    if (c->h_fe_maps_bytes < bytes) {
+      if (c->h_fe_maps) cudaFreeHost(c->h_fe_maps);
+      c->h_fe_maps = nullptr;
+      c->h_fe_maps_bytes = 0;
+      if (int e = c->cuda(cudaMallocHost((void**)&c->h_fe_maps, bytes), "faster-evgen map buffer")) return e;
+      c->h_fe_maps_bytes = bytes;
+    }
+    dst = c->h_fe_maps;
+    *pinned = dst;
+  } else {
+    maps->resize(n * kFeEntries);
+    dst = maps->data();
+  }
+  st = c->cuda(cudaMemcpyAsync(dst, c->d_fe_map, bytes, cudaMemcpyDeviceToHost, stream), "copy faster-evgen maps");
   if (!st) st = c->cuda(cudaStreamSynchronize(stream), "faster-evgen map pass");
   return st;
 }
@@ -439,7 +457,8 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
 // Steps 1-2 for `streams`: composes chunks until each stream's target.
 int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cudaStream_t stream) {
   std::vector<FeChunk> descs;
-  std::vector<uint32_t> maps, one;
+  std::vector<uint32_t> one;
+  const uint32_t* maps = nullptr;  // the launch's maps, in the pinned buffer
   for (;;) {
     descs.clear();
     for (FeStream& s : streams) {
@@ -453,7 +472,7 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
       if (descs.size() >= kFeMapLaunch) break;
     }
     if (descs.empty()) return TP_OK;
-    if (int st = fe_launch(c, fp, descs, true, stream, &maps)) return st;
+    if (int st = fe_launch(c, fp, descs, true, stream, nullptr, &maps)) return st;
     size_t d = 0;
     for (FeStream& s : streams) {
       while (d < descs.size() && descs[d].stream == s.id && descs[d].chunk == s.next_chunk && !s.done()) {
@@ -700,6 +719,7 @@ void tp_destroy(tp_ctx* c) {
                   c->d_fe_cstate, c->d_fe_map, c->d_fe_tstate, c->d_fe_store};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  if (c->h_fe_maps) cudaFreeHost(c->h_fe_maps);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->pts.exec) cudaGraphExecDestroy(c->pts.exec);
   if (c->pts.graph) cudaGraphDestroy(c->pts.graph);
