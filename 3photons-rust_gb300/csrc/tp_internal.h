@@ -127,9 +127,10 @@ struct PointsParams {
 // A stream's draw positions are cut into chunks of kFeChunk; an event
 // belongs to the chunk of its first draw. A chunk's CTA (two warps)
 // computes the accept bits of kFeSpan positions (the chunk and a margin for
-// the events that run past its end), 576 per xoshiro lane.
+// the events that run past its end: 2048 draws, an event of a thousand
+// re-rolls), 544 per xoshiro lane.
 constexpr uint32_t kFeChunk = 32768;
-constexpr uint32_t kFeSpan = 36864;
+constexpr uint32_t kFeSpan = 34816;
 constexpr int kFeThreads = 64;  // threads of the chunk kernels
 constexpr uint32_t kFeLaneSpan = kFeSpan / kFeThreads;
 constexpr int kFeEntries = 32;             // entry offsets per chunk map
@@ -196,7 +197,7 @@ constexpr uint32_t kFeStoreExit = kFeStoreCanon + kFeChunk / 32;
 constexpr uint32_t kFeStoreTrace = kFeStoreExit + kFeSubs;
 constexpr uint32_t kFeStoreEntry = kFeStoreTrace + kFeSubs * kFeEntries;
 constexpr uint32_t kFeStoreWords = kFeStoreEntry + 4;
-// xoshiro checkpoints per lane: the states at 576 l + 128 k + 3, k < 5
+// xoshiro checkpoints per lane: the states at 544 l + 128 k + 3, k < 5
 constexpr uint32_t kFeCkpts = (kFeLaneSpan / 32 + 3) / 4;
 
 // per-bin record of the binned forward pass
