@@ -391,7 +391,7 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // One stream (events numbered through the run) or one per batch
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
-constexpr uint64_t kFeMapLaunch = 65536;  // chunks per map launch
+constexpr uint64_t kFeMapLaunch = 1u << 19;  // chunks per map launch (~1e9 events)
 constexpr uint64_t kFeStoreCap = 16ull << 30;  // bytes of device memory for the bit store
 // batches per starts + events launch: bounds the thread start states to
 // 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
@@ -427,7 +427,14 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   fp.n_chunks = n;
   fp.chunk_state = c->d_fe_cstate;
   fp.map = static_cast<uint32_t*>(c->d_fe_map);
-  if (launch_fe_seed(fp, stream) != TP_OK)
+  // the starts pass of one-stream xoshiro chunks in the bit store reads
+  // their start states there (kept by the map pass): no seeding
+  bool seed = true;
+  if (!map_pass && fp.kind == TP_RNG_XOSHIRO256P && fp.bits_store && !fp.jpb) {
+    seed = false;
+    for (const FeChunk& d : descs) seed |= d.chunk >= fp.store_chunks;
+  }
+  if (seed && launch_fe_seed(fp, stream) != TP_OK)
     return c->fail(TP_ERR_CUDA, std::string("faster-evgen seed launch: ") + cudaGetErrorString(cudaGetLastError()));
   const int lst = map_pass ? launch_fe_map(fp, stream) : launch_fe_starts(fp, stream);
   if (lst != TP_OK)
@@ -467,6 +474,11 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
       // short guess maps the rest in the next round
       const double draws = fp.kind == TP_RNG_RANF ? 18.0 : 16.7;
       const uint64_t need = (uint64_t)((double)(s.target - s.events) * draws / kFeChunk) + 2;
+      if (streams.size() == 1) {  // one stream: room for the round's chunks at once, and a margin
+        const size_t round = (size_t)(need < kFeMapLaunch ? need : kFeMapLaunch);
+        descs.reserve(round);
+        s.chunks.reserve(s.chunks.size() + round + round / 32 + 64);
+      }
       for (uint64_t k = 0; k < need && descs.size() < kFeMapLaunch; ++k)
         descs.push_back(FeChunk{s.id, s.next_chunk + k, 0, 0, 0});
       if (descs.size() >= kFeMapLaunch) break;
@@ -541,7 +553,7 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     // for the starts pass when they fit in kFeStoreCap (xoshiro 15.7 GB and
     // ranf 9.9 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
-    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? kFeThreads * kFeCkpts * 4 * sizeof(uint64_t) : 0;
+    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? kFeCkptWords * sizeof(uint64_t) : 0;
     const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + ckpt_bytes;
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
@@ -555,18 +567,20 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     if (int st = fe_compose(c, fp, one, stream)) return st;
   }
   const uint64_t piece = kind == TP_RNG_RANF ? kFePieceRanf : kFePieceXo;
+  size_t kpos = 0;  // one stream: the first composed chunk that ends past the piece's first event
   for (uint64_t p0 = first_batch; p0 < b_end; p0 += piece) {
     const uint64_t pn = b_end - p0 < piece ? b_end - p0 : piece;
     std::vector<FeChunk> descs;
     if (!jpb) {
+      // the chunks holding events [lo, hi), in stream order (their first
+      // events ascend, and so do the pieces)
       const uint64_t lo = p0 * (uint64_t)kBatch;
       const uint64_t hi = (p0 + pn) * (uint64_t)kBatch;
       const std::vector<FeChunk>& ch = one[0].chunks;
-      for (size_t k = 0; k < ch.size(); ++k) {
-        const uint64_t f0 = ch[k].first_event;
-        const uint64_t f1 = k + 1 < ch.size() ? ch[k + 1].first_event : one[0].events;
-        if (f0 < hi && f1 > lo && f1 > f0) descs.push_back(ch[k]);
-      }
+      auto end_of = [&](size_t k) { return k + 1 < ch.size() ? ch[k + 1].first_event : one[0].events; };
+      while (kpos < ch.size() && end_of(kpos) <= lo) ++kpos;
+      for (size_t k = kpos; k < ch.size() && ch[k].first_event < hi; ++k)
+        if (end_of(k) > ch[k].first_event) descs.push_back(ch[k]);
     } else {
       std::vector<FeStream> streams(pn);
       for (uint64_t i = 0; i < pn; ++i) {

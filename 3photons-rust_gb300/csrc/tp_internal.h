@@ -197,8 +197,11 @@ constexpr uint32_t kFeStoreExit = kFeStoreCanon + kFeChunk / 32;
 constexpr uint32_t kFeStoreTrace = kFeStoreExit + kFeSubs;
 constexpr uint32_t kFeStoreEntry = kFeStoreTrace + kFeSubs * kFeEntries;
 constexpr uint32_t kFeStoreWords = kFeStoreEntry + 4;
-// xoshiro checkpoints per lane: the states at 544 l + 128 k + 3, k < 5
+// xoshiro checkpoints per lane: the states at 544 l + 128 k + 3, k < 5;
+// per chunk those of the kFeThreads lanes, then the chunk's start state
 constexpr uint32_t kFeCkpts = (kFeLaneSpan / 32 + 3) / 4;
+constexpr uint32_t kFeCkptStart = kFeThreads * kFeCkpts * 4;
+constexpr uint32_t kFeCkptWords = kFeCkptStart + 4;
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
