@@ -427,10 +427,10 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   fp.n_chunks = n;
   fp.chunk_state = c->d_fe_cstate;
   fp.map = static_cast<uint32_t*>(c->d_fe_map);
-  // the starts pass of one-stream xoshiro chunks in the bit store reads
-  // their start states there (kept by the map pass): no seeding
+  // the starts pass of one-stream chunks in the bit store steps from the
+  // checkpoints the map pass kept there: no seeding
   bool seed = true;
-  if (!map_pass && fp.kind == TP_RNG_XOSHIRO256P && fp.bits_store && !fp.jpb) {
+  if (!map_pass && fp.bits_store && !fp.jpb) {
     seed = false;
     for (const FeChunk& d : descs) seed |= d.chunk >= fp.store_chunks;
   }
@@ -472,7 +472,7 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
       if (s.done()) continue;
       // ~16.64 (xoshiro) or ~17.9 (ranf, block skips) draws per event; a
       // short guess maps the rest in the next round
-      const double draws = fp.kind == TP_RNG_RANF ? 18.0 : 16.7;
+      const double draws = fp.kind == TP_RNG_RANF ? 18.2 : 16.7;
       const uint64_t need = (uint64_t)((double)(s.target - s.events) * draws / kFeChunk) + 2;
       if (streams.size() == 1) {  // one stream: room for the round's chunks at once, and a margin
         const size_t round = (size_t)(need < kFeMapLaunch ? need : kFeMapLaunch);
@@ -549,19 +549,19 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     // batches past the run are empty: their event kernel CTAs store zeros
     const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
-    // the map pass keeps every chunk's accept bits (and xoshiro lane states)
-    // for the starts pass when they fit in kFeStoreCap (xoshiro 15.7 GB and
-    // ranf 9.9 GB per 1e9 events)
+    // the map pass keeps every chunk's accept bits, chases, walks and
+    // stream checkpoints for the starts pass when they fit in kFeStoreCap
+    // (xoshiro 15.7 GB and ranf 12.3 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
-    const size_t ckpt_bytes = kind == TP_RNG_XOSHIRO256P ? kFeCkptWords * sizeof(uint64_t) : 0;
+    const size_t ckpt_bytes =
+        kind == TP_RNG_XOSHIRO256P ? kFeCkptWords * sizeof(uint64_t) : kFeRanfCkptInts * sizeof(int32_t);
     const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + ckpt_bytes;
     if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
         return st;
       fp.bits_store = static_cast<uint32_t*>(c->d_fe_store);
-      fp.ckpt_store = ckpt_bytes ? reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) +
-                                                               chunks * kFeStoreWords * sizeof(uint32_t))
-                                 : nullptr;
+      fp.ckpt_store =
+          reinterpret_cast<uint64_t*>(static_cast<char*>(c->d_fe_store) + chunks * kFeStoreWords * sizeof(uint32_t));
       fp.store_chunks = chunks;
     }
     if (int st = fe_compose(c, fp, one, stream)) return st;

@@ -175,9 +175,9 @@ struct FeParams {
   void* thread_state;
   unsigned int* err;
   // one-stream runs: the map pass keeps each chunk's accept bits and
-  // sub-span chases (kFeStoreWords words) and, for xoshiro, its lanes'
-  // checkpoints (kFeThreads x kFeCkpts x 4 words) for the starts pass; chunks >=
-  // store_chunks (or a null store) regenerate them
+  // sub-span chases (kFeStoreWords words) and its stream checkpoints
+  // (xoshiro: kFeCkptWords u64, ranf: kFeRanfCkptInts i32) for the starts
+  // pass; chunks >= store_chunks (or a null store) regenerate them
   uint32_t* bits_store;
   uint64_t* ckpt_store;
   uint64_t store_chunks;
@@ -202,6 +202,12 @@ constexpr uint32_t kFeStoreWords = kFeStoreEntry + 4;
 constexpr uint32_t kFeCkpts = (kFeLaneSpan / 32 + 3) / 4;
 constexpr uint32_t kFeCkptStart = kFeThreads * kFeCkpts * 4;
 constexpr uint32_t kFeCkptWords = kFeCkptStart + 4;
+// ranf checkpoints per chunk: the block (slots 1..55 at [1..55] of 56
+// ints) after every kFeRanfCkptBlocks resets from the block holding the
+// chunk's first draw, through the chunk's last block (596 resets)
+constexpr uint32_t kFeRanfCkptBlocks = 32;
+constexpr uint32_t kFeRanfCkpts = (54 + kFeChunk - 1) / 55 / kFeRanfCkptBlocks + 1;
+constexpr uint32_t kFeRanfCkptInts = kFeRanfCkpts * 56;
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
