@@ -164,6 +164,7 @@ def library():
         "tp_dump_events_prec": (i32, [vp, P(CConfig), i32, u64, u64, u64, i32, vp]),
         "tp_set_events_per_thread": (i32, [vp, i32]),
         "tp_set_occupancy": (i32, [vp, i32, i32]),
+        "tp_set_fe_store_cap": (i32, [vp, u64]),
         "tp_get_tuning": (i32, [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "tp_profile": (i32, [vp, i32]),
         "tp_profile_read": (i32, [vp, P(ctypes.c_double), P(ctypes.c_uint64), P(ctypes.c_double), P(ctypes.c_uint64)]),
@@ -406,6 +407,11 @@ class Context:
     def set_occupancy(self, precision, min_ctas_per_sm):
         """xoshiro event kernel variant of `precision`: 2 or 3 CTAs per SM."""
         self.check(library().tp_set_occupancy(self.h, precision, min_ctas_per_sm))
+
+    def set_fe_store_cap(self, nbytes):
+        """Device memory faster-evgen one-stream runs may keep between their
+        boundary passes (0: recompute instead)."""
+        self.check(library().tp_set_fe_store_cap(self.h, nbytes))
 
     def tuning(self, precision):
         """(events per thread, kernel variant) in use for `precision`."""

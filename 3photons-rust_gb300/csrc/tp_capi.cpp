@@ -128,6 +128,7 @@ struct tp_ctx {
   void* d_fe_store = nullptr;  // one-stream runs: accept bits and lane states per chunk
   uint32_t* h_fe_maps = nullptr;  // pinned host copy of a map launch's maps
   size_t h_fe_maps_bytes = 0;
+  uint64_t fe_store_cap = 16ull << 30;  // bytes the bit store may take
   size_t fe_store_bytes = 0;
   int sms = 0;
   // batched form (tp_run_points): device buffers and the captured graph
@@ -392,7 +393,6 @@ int run_async(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint
 // (TP_MODE_JUMP_PER_BATCH: events numbered within the batch).
 // ---------------------------------------------------------------------------
 constexpr uint64_t kFeMapLaunch = 1u << 19;  // chunks per map launch (~1e9 events)
-constexpr uint64_t kFeStoreCap = 16ull << 30;  // bytes of device memory for the bit store
 // batches per starts + events launch: bounds the thread start states to
 // 134 MB (xoshiro, 32 B per thread) and 235 MB (ranf, 224 B per thread)
 constexpr uint64_t kFePieceXo = 16384, kFePieceRanf = 4096;
@@ -550,13 +550,13 @@ int run_fe(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t seed, uint64_
     const uint64_t e_end = b_end * (uint64_t)kBatch < n_total ? b_end * (uint64_t)kBatch : n_total;
     one[0].target = first_batch * (uint64_t)kBatch < n_total ? e_end : 0;
     // the map pass keeps every chunk's accept bits, chases, walks and
-    // stream checkpoints for the starts pass when they fit in kFeStoreCap
-    // (xoshiro 15.7 GB and ranf 12.3 GB per 1e9 events)
+    // stream checkpoints for the starts pass when they fit in the context's
+    // store cap (xoshiro 15.7 GB and ranf 12.3 GB per 1e9 events)
     const uint64_t chunks = (uint64_t)((double)one[0].target * 18.5 / kFeChunk) + 64;
     const size_t ckpt_bytes =
         kind == TP_RNG_XOSHIRO256P ? kFeCkptWords * sizeof(uint64_t) : kFeRanfCkptInts * sizeof(int32_t);
     const size_t per_chunk = kFeStoreWords * sizeof(uint32_t) + ckpt_bytes;
-    if (one[0].target > 0 && (double)chunks * per_chunk <= (double)kFeStoreCap) {
+    if (one[0].target > 0 && (double)chunks * per_chunk <= (double)c->fe_store_cap) {
       if (int st = ensure(c, &c->d_fe_store, &c->fe_store_bytes, chunks * per_chunk, "faster-evgen bit store"))
         return st;
       fp.bits_store = static_cast<uint32_t*>(c->d_fe_store);
@@ -819,6 +819,12 @@ int tp_dump_events_prec(tp_ctx* c, const tp_config* cfg, int rng_kind, uint64_t 
   if (!st) st = c->cuda(cudaStreamSynchronize(c->stream), "dump events");
   if (!st && herr) return c->fail(TP_ERR_UNSUPPORTED, "ranf batch seed outside [0, 1e9): no jump-ahead");
   return st;
+}
+
+int tp_set_fe_store_cap(tp_ctx* c, uint64_t bytes) {
+  if (!c) return TP_ERR_INVALID;
+  c->fe_store_cap = bytes;
+  return TP_OK;
 }
 
 int tp_set_events_per_thread(tp_ctx* c, int ept) {

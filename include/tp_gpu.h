@@ -222,6 +222,14 @@ int tp_set_events_per_thread(tp_ctx *ctx, int ept);
  * the same either way. */
 int tp_set_occupancy(tp_ctx *ctx, int precision, int min_ctas_per_sm);
 
+/* Memory: the device memory (bytes) that faster-evgen one-stream runs may
+ * keep between their two boundary passes (per chunk of 32 768 draws its
+ * accept bits, chases and stream checkpoints; about 16 GB per 1e9 events).
+ * Default 16 GiB; a run whose store would not fit computes them a second
+ * time instead (slower, same results); 0 never keeps them. No counterpart
+ * in the reference. */
+int tp_set_fe_store_cap(tp_ctx *ctx, uint64_t bytes);
+
 /* Tuning in use for `precision`: events per thread and kernel variant
  * (minimum resident CTAs per SM), as set or picked by tp_autotune. */
 int tp_get_tuning(tp_ctx *ctx, int precision, int *ept, int *min_ctas_per_sm);

@@ -71,4 +71,5 @@ def test_null_context_rejected(tp):
     assert lib.tp_run_batches(None, ctypes.byref(cfg), 0, 0, 0, 1, 0, ctypes.byref(soa)) == tp.TP_ERR_INVALID
     assert lib.tp_dump_events(None, ctypes.byref(cfg), 0, 0, 0, 1, None) == tp.TP_ERR_INVALID
     assert lib.tp_get_tuning(None, 0, None, None) == tp.TP_ERR_INVALID
+    assert lib.tp_set_fe_store_cap(None, 0) == tp.TP_ERR_INVALID
     assert lib.tp_grad(None, ctypes.byref(cfg), 0, 0, 0, 1, 0, None, None, None, None) == tp.TP_ERR_INVALID

@@ -106,6 +106,27 @@ def test_unsupported_combinations(tp, ctx, cfg_valeurs):
     ctx.run_batches(cfg, 0, 1, rng="xoshiro", faster_evgen=True)
 
 
+@pytest.mark.parametrize("rng", ["xoshiro", "ranf"])
+def test_without_the_bit_store(tp, oracle, ctx, cfg_valeurs, rng):
+    """One-stream runs keep each chunk's accept bits, chases, walks and
+    stream checkpoints between the map and starts passes; with the store
+    off (tp_set_fe_store_cap(0), as for runs too large for it) the starts
+    pass computes them again: identical batches, bit for bit, and the
+    restatement's."""
+    cfg = cfg_valeurs.replace(num_events=654_321)
+    nb = cfg.num_batches
+    kept = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True)
+    ctx.set_fe_store_cap(0)
+    try:
+        again = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True)
+        part = ctx.run_batches(cfg, 17, 30, rng=rng, faster_evgen=True)
+    finally:
+        ctx.set_fe_store_cap(16 << 30)
+    assert kept.as_array().tobytes() == again.as_array().tobytes()
+    assert_batches_close(again, oracle_batches(tp, oracle, cfg, 0, nb, rng, False, True))
+    assert_batches_close(part, oracle_batches(tp, oracle, cfg, 17, 30, rng, False, True))
+
+
 @pytest.mark.parametrize("seed", [42049, 176937])
 def test_chunk_entered_past_the_mapped_offsets(tp, oracle, ctx, cfg_valeurs, seed):
     """Chunk maps cover entry offsets 0..31. These xoshiro seeds (found by
