@@ -415,7 +415,7 @@ int fe_launch(tp_ctx* c, FeParams fp, const std::vector<FeChunk>& descs, bool ma
   const size_t n = descs.size();
   if (n == 0) return TP_OK;
   if (int st = ensure(c, &c->d_fe_chunks, &c->fe_chunks_bytes, n * sizeof(FeChunk), "faster-evgen chunks")) return st;
-  if (int st = ensure(c, &c->d_fe_cstate, &c->fe_cstate_bytes, n * 56 * sizeof(int32_t), "faster-evgen chunk states"))
+  if (int st = ensure(c, &c->d_fe_cstate, &c->fe_cstate_bytes, n * 112 * sizeof(int32_t), "faster-evgen chunk states"))
     return st;
   if (map_pass)
     if (int st = ensure(c, &c->d_fe_map, &c->fe_map_bytes, n * kFeEntries * sizeof(uint32_t), "faster-evgen maps"))

@@ -165,7 +165,8 @@ struct FeParams {
   const uint64_t* xo_lane_tab;   // x^(kFeLaneSpan l), l < kFeThreads, as jump tables (kJumpTabWords each)
   const FeChunk* chunks;
   uint64_t n_chunks;
-  void* chunk_state;             // per chunk: xoshiro 4 x u64, ranf 56 x i32
+  void* chunk_state;             // per chunk: xoshiro 4 x u64; ranf 2 x 56 i32, at the chunk's
+                                 // start and at position kFeSpan / 2 (the map pass's two warps)
   uint32_t* map;                 // map pass: [n_chunks][32] exit << 16 | events
   // starts pass: thread t of batch first_batch + i starts event
   // kBatch (first_batch + i) + ept t; its stream state goes to
