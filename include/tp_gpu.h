@@ -84,8 +84,10 @@ extern "C" {
  * FP32 physics with the certified cuts), batch
  * accumulators only (tp_run_batches / tp_run_batches_async); the _async call
  * waits for the boundary pass before it queues the event kernels. A
- * one-stream run keeps the pass's accept bits in device memory (about 5.8 GB
- * per 1e9 events, not above 8 GiB; longer runs recompute them). */
+ * one-stream run keeps the pass's accept bits, chases and stream
+ * checkpoints in device memory between its two halves (about 16 GB per
+ * 1e9 xoshiro events, 12 GB ranf; budget: tp_set_fe_store_cap, default
+ * 16 GiB; larger runs recompute them). */
 #define TP_RNG_RANF 0
 #define TP_RNG_XOSHIRO256P 1
 #define TP_RNG_KIND_MASK 0xff
