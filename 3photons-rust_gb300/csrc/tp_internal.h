@@ -136,11 +136,11 @@ constexpr uint32_t kFeLaneSpan = kFeSpan / kFeThreads;
 constexpr int kFeEntries = 32;             // entry offsets per chunk map
 constexpr uint32_t kFeMapError = 0xffffffffu;
 constexpr int kFeMaxStarts = 128;          // thread starts recorded per chunk
-constexpr int kFeMaxTries = 2048;          // re-rolls per point (the span holds fewer)
+constexpr int kFeMaxTries = 2048;          // re-rolls per point: an event stops after 3 kFeMaxTries
 // error bits set by the faster-evgen kernels
 constexpr unsigned kFeErrSpan = 0x10u;     // an event ran past the chunk's span
 constexpr unsigned kFeErrStarts = 0x20u;   // too many thread starts in a chunk
-constexpr unsigned kFeErrTries = 0x40u;    // a point was re-rolled kFeMaxTries times
+constexpr unsigned kFeErrTries = 0x40u;    // an event re-rolled its points 3 kFeMaxTries times
 
 // One chunk of a stream: for the map pass, lane l maps entry offset
 // entry + l; for the starts pass, entry is the offset of the chunk's first
