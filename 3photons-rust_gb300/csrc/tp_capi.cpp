@@ -37,7 +37,7 @@ struct Tables {
   std::vector<uint64_t> xo_batch, xo_jump, xo_draw;  // 64 x 4 words each
   std::vector<uint64_t> xo_fe_chunk;                  // 64 x 4: x^(kFeChunk 2^k)
   std::vector<uint64_t> xo_fe_lane;                   // kFeThreads x 4: x^(kFeLaneSpan l)
-  std::vector<uint32_t> ranf;                         // 64 x 55
+  std::vector<uint32_t> ranf;                         // kRanfTableRows x 55
 };
 
 const Tables& host_tables() {
@@ -71,11 +71,16 @@ const Tables& host_tables() {
       for (int w = 0; w < 4; ++w) t.xo_fe_lane[4 * l + w] = cur.w[w];
       cur = gf2_mulmod(cur, lane_step);
     }
-    t.ranf.resize(64 * 55);
+    t.ranf.resize(kRanfTableRows * 55);
     RanfPoly r = ranf_xpow(55);
     for (int k = 0; k < 64; ++k) {
       for (int i = 0; i < 55; ++i) t.ranf[55 * k + i] = r.c[i];
       r = ranf_mulmod(r, r);
+    }
+    const uint64_t steps[4] = {595, 596, 316, 317};
+    for (int k = 0; k < 4; ++k) {
+      const RanfPoly s = ranf_xpow(55 * steps[k]);
+      for (int i = 0; i < 55; ++i) t.ranf[55 * (kFeRanfStepRow + k) + i] = s.c[i];
     }
   });
   return t;
@@ -680,7 +685,7 @@ tp_ctx* tp_create(int device, int* status) {
   alloc((void**)&c->d_xo_batch, 256 * 8, "tables");
   alloc((void**)&c->d_xo_jump, 256 * 8, "tables");
   alloc((void**)&c->d_xo_draw, 256 * 8, "tables");
-  alloc((void**)&c->d_ranf_tab, 64 * 55 * 4, "tables");
+  alloc((void**)&c->d_ranf_tab, kRanfTableRows * 55 * 4, "tables");
   // the binned passes (slot 2) jump by polynomial: no table
   for (int k = 0; k < 3; ++k) alloc((void**)&c->d_thread_poly[k], kTpb * 32, "tables");
   for (int k = 0; k < 2; ++k) alloc((void**)&c->d_jump_tab[k], (size_t)kTpb * kJumpTabWords * 8, "jump tables");
@@ -700,7 +705,8 @@ tp_ctx* tp_create(int device, int* status) {
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_batch, t.xo_batch.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_jump, t.xo_jump.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st) st = c->cuda(cudaMemcpy(c->d_xo_draw, t.xo_draw.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
-  if (!st) st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), 64 * 55 * 4, cudaMemcpyHostToDevice), "tables");
+  if (!st)
+    st = c->cuda(cudaMemcpy(c->d_ranf_tab, t.ranf.data(), kRanfTableRows * 55 * 4, cudaMemcpyHostToDevice), "tables");
   if (!st)
     st = c->cuda(cudaMemcpy(c->d_xo_fe_chunk, t.xo_fe_chunk.data(), 256 * 8, cudaMemcpyHostToDevice), "tables");
   if (!st)

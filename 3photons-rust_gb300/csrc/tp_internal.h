@@ -209,6 +209,12 @@ constexpr uint32_t kFeCkptWords = kFeCkptStart + 4;
 constexpr uint32_t kFeRanfCkptBlocks = 32;
 constexpr uint32_t kFeRanfCkpts = (54 + kFeChunk - 1) / 55 / kFeRanfCkptBlocks + 1;
 constexpr uint32_t kFeRanfCkptInts = kFeRanfCkpts * 56;
+// ranf: rows kFeRanfStepRow.. of the x^(55 2^k) table hold x^(55 n) for the
+// block distances n = 595, 596 between consecutive chunks' first draws and
+// n = 316, 317 from a chunk's first draw to its second state (kFeSpan / 2 on)
+constexpr int kFeRanfStepRow = 64;
+constexpr int kRanfTableRows = kFeRanfStepRow + 4;
+static_assert(kFeChunk / 55 == 595 && (kFeSpan / 2) / 55 == 316, "ranf chunk step table");
 
 // per-bin record of the binned forward pass
 constexpr int kBinStride = 8;  // raw sums R_0..R_4, events, sum w, sum w^2
