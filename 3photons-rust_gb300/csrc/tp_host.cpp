@@ -257,6 +257,7 @@ int make_ev_const(const tp_config& cfg, int flags, EvConst* out) {
   k.f_half = (float)k.half;
   k.f_em_x = (float)k.em_x;
   k.f_acut = (float)k.acut;
+  k.f_acut_half = (float)(k.acut * k.half);
   k.f_bcut = (float)k.bcut;
   k.f_emin = (float)k.emin;
   k.f_sincut = (float)k.sincut;

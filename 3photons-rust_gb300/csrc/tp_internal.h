@@ -39,6 +39,7 @@ struct EvConst {
   double sc_raw[4];
   // FP32 copies for the mixed-precision path
   float f_e_total, f_half, f_em_x, f_acut, f_bcut, f_emin, f_sincut;
+  float f_acut_half;  // acut * half rounded once (the beam cut's threshold per unit of E)
   float f_xx_in, f_fx_em, f_fx_ep, f_c1, f_c2;
   // The FP32 helicity sums are computed from momenta scaled by 1 / lambda,
   // lambda = 2^ceil(log2(sqrt(s) / 2)) (exact), and come out as raw_c /
