@@ -56,6 +56,19 @@ def test_batch_range_inside_the_run(tp, oracle, ctx, cfg_valeurs, rng, jump):
     assert_batches_close(tail, oracle_batches(tp, oracle, cfg, 38, 4, rng, jump, True))
 
 
+@pytest.mark.parametrize("rng,jump", [("ranf", False), ("xoshiro", False), ("ranf", True)])
+def test_fp32_mixed_batch_range_equals_the_full_run(tp, ctx, cfg_valeurs, rng, jump):
+    """FP32-mixed: a batch range inside the run gives the full run's batches
+    bit for bit (its events, start states and per-batch sums do not depend
+    on the range asked for)."""
+    cfg = cfg_valeurs.replace(num_events=400_000)
+    full = ctx.run_batches(cfg, 0, cfg.num_batches, rng=rng, jump_per_batch=jump, faster_evgen=True,
+                           precision=tp.TP_PREC_FP32_MIXED)
+    part = ctx.run_batches(cfg, 23, 9, rng=rng, jump_per_batch=jump, faster_evgen=True,
+                           precision=tp.TP_PREC_FP32_MIXED)
+    assert part.as_array().tobytes() == full.as_array()[23:32].tobytes()
+
+
 @pytest.mark.parametrize("ept", [40, 64, 333, 10000])
 def test_events_per_thread_invariance(tp, oracle, cfg_valeurs, ept):
     cfg = cfg_valeurs.replace(num_events=50_001)
@@ -116,13 +129,17 @@ def test_without_the_bit_store(tp, oracle, ctx, cfg_valeurs, rng):
     cfg = cfg_valeurs.replace(num_events=654_321)
     nb = cfg.num_batches
     kept = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True)
+    kept32 = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True, precision=tp.TP_PREC_FP32_MIXED)
     ctx.set_fe_store_cap(0)
     try:
         again = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True)
+        again32 = ctx.run_batches(cfg, 0, nb, rng=rng, faster_evgen=True, precision=tp.TP_PREC_FP32_MIXED)
         part = ctx.run_batches(cfg, 17, 30, rng=rng, faster_evgen=True)
     finally:
         ctx.set_fe_store_cap(16 << 30)
     assert kept.as_array().tobytes() == again.as_array().tobytes()
+    assert kept32.as_array().tobytes() == again32.as_array().tobytes()
+    assert np.array_equal(kept32.selected, kept.selected)
     assert_batches_close(again, oracle_batches(tp, oracle, cfg, 0, nb, rng, False, True))
     assert_batches_close(part, oracle_batches(tp, oracle, cfg, 17, 30, rng, False, True))
 
