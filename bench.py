@@ -290,9 +290,12 @@ def issue_roofline(torch, dev, fp32, clocks):
         return
     prof = json.load(open(path))
     peak = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * clocks["sm_mhz"] * 1e6
-    achieved = prof["warp_inst_per_event"] * fp32["kernel_events_per_s"]
+    # the count of the variant this run used (the variants spill differently)
+    per_event = prof.get("by_variant", {}).get(str(fp32.get("kernel_variant_ctas_per_sm")),
+                                              prof["warp_inst_per_event"])
+    achieved = per_event * fp32["kernel_events_per_s"]
     fp32["roofline"]["issue"] = {"achieved": achieved, "peak": peak, "unit": "warp instructions/s",
-                                 "frac": achieved / peak, "warp_inst_per_event": prof["warp_inst_per_event"],
+                                 "frac": achieved / peak, "warp_inst_per_event": per_event,
                                  "source": prof["source"]}
 
 
