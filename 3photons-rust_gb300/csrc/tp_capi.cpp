@@ -496,7 +496,19 @@ int fe_compose(tp_ctx* c, const FeParams& fp, std::vector<FeStream>& streams, cu
         uint32_t m;
         if (s.entry < (uint32_t)kFeEntries) {
           m = maps[d * kFeEntries + s.entry];
-        } else {  // the chunk is entered past the 32 mapped offsets: map that offset alone
+        } else if (fp.bits_store && !fp.jpb && s.next_chunk < fp.store_chunks) {
+          // entered past the 32 mapped offsets, a kept chunk: walk from its
+          // offset over what the map pass stored (the starts pass then walks
+          // this chunk itself)
+          uint32_t* d_out = static_cast<uint32_t*>(c->d_fe_map);
+          int st = launch_fe_walk_kept(fp, s.next_chunk, s.entry, d_out, stream);
+          if (st)
+            return c->fail(TP_ERR_CUDA,
+                           std::string("faster-evgen walk launch: ") + cudaGetErrorString(cudaGetLastError()));
+          st = c->cuda(cudaMemcpyAsync(&m, d_out, sizeof m, cudaMemcpyDeviceToHost, stream), "faster-evgen walk");
+          if (!st) st = c->cuda(cudaStreamSynchronize(stream), "faster-evgen walk");
+          if (st) return st;
+        } else {  // entered past the 32 mapped offsets: map that offset alone
           std::vector<FeChunk> single{FeChunk{s.id, s.next_chunk, 0, s.entry, 0}};
           if (int st = fe_launch(c, fp, single, true, stream, &one)) return st;
           m = one[0];

@@ -256,6 +256,8 @@ int launch_adjoint(int rng_kind, const KParams& p, int tpb, void* stream);
 int launch_fe_seed(const FeParams& p, void* stream);
 int launch_fe_map(const FeParams& p, void* stream);
 int launch_fe_starts(const FeParams& p, void* stream);
+// one kept chunk's map from an entry offset >= kFeEntries, from the store
+int launch_fe_walk_kept(const FeParams& p, uint64_t chunk, uint32_t entry, uint32_t* d_out, void* stream);
 int launch_fe_events(int rng_kind, const KParams& p, int tpb, void* stream);
 
 }  // namespace tp
