@@ -31,6 +31,8 @@ def test_profile_figures():
     assert t["kernel"] == "k_events_xoshiro_fp64" and 0 < t["bytes_per_event"] < 1
     i = json.load(open(os.path.join(ROOT, "profiles", "issue.json")))
     assert i["kernel"] == "k_events_xoshiro_fp32" and 10 < i["warp_inst_per_event"] < 100
+    # per kernel variant (CTAs per SM), as the bench looks them up
+    assert set(i["by_variant"]) <= {"2", "3", "4"} and all(10 < v < 100 for v in i["by_variant"].values())
     for f in (t["source"].split(":")[0], i["source"].split(":")[0]):
         assert os.path.exists(os.path.join(ROOT, f)), f
 
